@@ -1,0 +1,427 @@
+"""Benchmark of the batched Rosenbrock stiff-chemistry integrator on GB300.
+
+Workload (one "step" = one pass of the hot path over one batch): the shipped
+17-species humid-air mechanism, 1,048,576 independent cells integrated over
+10 s at rtol 1e-4 / atol 1e-12 mol/L with Rodas3 -- seeded synthetic initial
+states (T ~ U[288, 303] K, c ~ 10^U[-12, -2] mol/L, H2O 55.5 mol/L). The metric
+is cell-integrations/s (one cell advanced over the whole interval in one call).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+                    [--cells C] [--duration S] [--precision mixed|f64]
+
+value  : whole-job throughput with inputs resident in HBM (device-timed, CUDA
+         events around each step on the module stream, max over ranks)
+e2e    : the same metric through the C ABI with host buffers -- every step
+         copies the whole zone block host->device and the solver-written rows
+         back (the reference's dbd_advance_gpu call pattern)
+Both precisions run: `value` is the mixed path (FP32 RHS/Jacobian/LU with an
+FP64-residual refinement, FP64 state and step control); the plain FP64 path,
+bit-identical to the reference's CPU solver, is reported under "fp64".
+
+--impl reference times the reference algorithm on the host cores (the oracle
+restatement, pinned bit for bit to the reference's CPU solver) on a bounded
+sample of the same workload.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+HBM_FALLBACK_GBS = 6800.0
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cells", type=int, default=1 << 20)
+    ap.add_argument("--duration", type=float, default=10.0)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "f64"])
+    ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--seed", type=int, default=1)
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas: each rank integrates its own cells; no collective on the data path)
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+class Group:
+    def __init__(self, world):
+        self.world = world
+        self.pg = None
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.init_process_group("gloo")
+            self.dist = dist
+
+    def barrier(self):
+        if self.world > 1:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.world == 1:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.world > 1:
+            self.dist.destroy_process_group()
+
+
+# ---------------------------------------------------------------------------
+# clocks during the timed region
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.QUERY}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons, power = [], [], set(), []
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+                power.append(float(parts[3]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)), "reasons": sorted(reasons),
+                "samples": len(sm), "power_w_median": float(np.median(power))}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic work per Rodas3 step, counted from the mechanism's tables
+# (FMA = 2 flops, mul/add/div/sqrt = 1)
+
+def flops_per_step(model) -> dict:
+    import ctypes as C
+
+    km = model.kinmech()
+    n, R = km.species_count, km.reaction_count
+    s_react = s_net = s_rn = s_rr = 0
+    for r in range(R):
+        rx = km.reactions[r]
+        s_react += rx.reactant_count
+        s_net += rx.net_count
+        s_rn += rx.reactant_count * rx.net_count
+        s_rr += rx.reactant_count * (rx.reactant_count - 1)
+    lower, upper = km.lower_begin[n], km.upper_begin[n]
+    fun = s_react + 2 * s_net
+    jac = s_rr + 2 * s_rn
+    lu = km.lu_div_count + 2 * km.lu_sub_count + 2 * n          # divs (mul), updates (fma), diag add + divide
+    solve = 2 * (lower + upper) + n
+    combo = 2 * 13 * n                                           # Rodas3 nonzero a, c, m, e: 3 + 6 + 3 + 1 FMAs per species
+    control = 8 * n                                              # scale fma, divide, square fma, max/abs, clamp
+    total = 4 * fun + jac + lu + 4 * solve + combo + control
+    return {"fun": fun, "neg_jac": jac, "factor": lu, "solve": solve, "total": total}
+
+
+def hbm_bytes_per_cell(n: int, R: int) -> int:
+    # read y, k, src, h, failed, period/first/count once; write y, h, steps, rejects, failed once
+    return 8 * (2 * n + R + n + 6)
+
+
+def measured_hbm_peak():
+    try:
+        with open(MEASURED_PEAKS) as f:
+            return float(json.load(f)["hbm_gbs"]), "MEASURED_PEAKS.json hbm_gbs (measured)"
+    except (OSError, KeyError, ValueError):
+        return HBM_FALLBACK_GBS, "fallback 6.8 TB/s"
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the reference algorithm (oracle restatement) on the host cores
+
+def cpu_baseline(cells_total: int, duration: float, seed: int, target_s: float, first_cell: int = 0):
+    import simstack_gb300 as sg
+    from oracle import oracle as O
+
+    O.build()
+    mech = O.Mechanism.air()
+    threads = os.cpu_count() or 1
+    # calibrate on a small sample, then size the timed sample to ~target_s
+    probe_cells = max(64, 8 * threads)
+    z = sg.air_cells(probe_cells, seed=seed, first_cell=first_cell)
+    t0 = time.perf_counter()
+    mech.advance("rodas3", O.control(), z.as_dict(), z.padded, 0, probe_cells, duration, 0, threads)
+    per_cell = (time.perf_counter() - t0) / probe_cells
+    cells = int(min(cells_total, max(probe_cells, target_s / max(per_cell, 1e-9))))
+    cells = max(64, cells // 64 * 64)
+    z = sg.air_cells(cells, seed=seed, first_cell=first_cell)
+    t0 = time.perf_counter()
+    mech.advance("rodas3", O.control(), z.as_dict(), z.padded, 0, cells, duration, 0, threads)
+    wall = time.perf_counter() - t0
+    return {"value": cells / wall, "unit": "cell-integrations/s", "cores": threads, "kind": "port",
+            "sample": f"first {cells} cells of the workload (same seeded inputs), {duration:g} s each, "
+                      f"{threads} host threads, {wall:.1f} s wall; oracle/kin_oracle.cpp (the reference's FP64 "
+                      f"algorithm, bit-identical to its CPU path)",
+            "wall_s": wall, "cells": cells}
+
+
+# ---------------------------------------------------------------------------
+
+def run_reference(args):
+    world, rank, local = dist_env()
+    if rank != 0:
+        return
+    cb = cpu_baseline(args.cells, args.duration, args.seed, args.cpu_seconds)
+    # `steps` timed samples of the same bounded workload, after warm-up
+    import simstack_gb300 as sg
+    from oracle import oracle as O
+
+    mech = O.Mechanism.air()
+    cells, threads = cb["cells"], cb["cores"]
+    times = []
+    for it in range(args.warmup + args.steps):
+        if it < args.warmup and it > 0:
+            continue   # the calibration run above already warmed the caches
+        z = sg.air_cells(cells, seed=args.seed)
+        t0 = time.perf_counter()
+        mech.advance("rodas3", O.control(), z.as_dict(), z.padded, 0, cells, args.duration, 0, threads)
+        times.append(time.perf_counter() - t0)
+    times = times[-args.steps:]
+    value = cells / float(np.mean(times))
+    line = {"metric": "cell-integrations/s", "value": value, "unit": "cell-integrations/s", "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times)) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"shipped 17-species air mechanism, {cells} of {args.cells} cells x "
+                                   f"{args.duration:g} s, Rodas3 rtol 1e-4 (bounded CPU sample)",
+                       "cells": cells, "duration_s": args.duration},
+            "cpu_baseline": {"value": value, "unit": "cell-integrations/s", "cores": threads, "kind": "port",
+                             "sample": cb["sample"]},
+            "e2e": {"value": value, "unit": "cell-integrations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_ours(args):
+    import ctypes as C
+
+    import simstack_gb300 as sg
+
+    world, rank, local = dist_env()
+    grp = Group(world)
+    L = sg.lib()
+    cells = args.cells
+    model = sg.Model.air()
+    km = model.kinmech()
+    flops = flops_per_step(model)
+    n, R = 17, 44
+
+    z = sg.air_cells(cells, seed=args.seed, first_cell=rank * cells)
+    block_bytes = z.nbytes
+    arena = 3 * block_bytes + (256 << 20)
+    mod = sg.Module(local, arena)
+    mod.set_mech(km, sg.method("rodas3"), sg.control())
+    pristine = mod.upload(z)
+    work = mod.alloc(block_bytes)
+    launch = z.launch(work, 0, args.duration)
+
+    def restore():   # fresh inputs for the next pass: device-to-device, on the module stream
+        sg.check(L.gpu_copy_on_device(work, pristine, block_bytes), "gpu_copy_on_device")
+
+    def timed_pass(precision: int, steps: int, warmup: int):
+        launch.precision = precision
+        kern = []
+        for it in range(warmup):
+            restore()
+            mod.advance(launch)
+        grp.barrier()
+        sg.check(L.gpu_sync(), "sync")
+        n0 = mod.launches()
+        t0 = time.perf_counter()
+        for it in range(steps):
+            restore()
+            kern.append(mod.advance(launch))
+        sg.check(L.gpu_sync(), "sync")
+        wall = time.perf_counter() - t0
+        grp.barrier()
+        return wall, kern, mod.launches() - n0
+
+    # step counts of the FP64 path (bit-identical to the oracle): the algorithmic work
+    restore()
+    mod.advance(launch)
+    zc = z.copy()
+    mod.download(zc, work)
+    steps_total = float(zc["steps"][:cells].sum() + zc["rejects"][:cells].sum())
+    failed = int(zc["failed"][:cells].sum())
+
+    # autotune the launch shape once per precision (persistent queue kernel)
+    tuned = {}
+    for prec in (0, 2):
+        restore()
+        launch.precision = prec
+        t = mod.autotune(launch, kind=1)
+        tuned[prec] = {"block": t.block, "variant": t.variant, "ms": t.ms}
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    wall64, kern64, l64 = timed_pass(0, args.steps, args.warmup)
+    wallmx, kernmx, lmx = timed_pass(2, args.steps, args.warmup)
+    clk = clocks.stop()
+
+    # accuracy of the mixed result on this batch vs the FP64 result (bit-identical to the oracle)
+    zm = z.copy()
+    mod.download(zm, work)
+    atol = sg.ATOL_1E12_MOLAR
+    rel = np.abs(zm["y"][:, :cells] - zc["y"][:, :cells]) / np.maximum(np.abs(zc["y"][:, :cells]), atol)
+
+    # end-to-end through the C ABI with host buffers (pinned), per step
+    sg.check(L.gpu_host_register(z.data.ctypes.data, z.nbytes), "gpu_host_register")
+    e2e_prec = 2 if args.precision == "mixed" else 0
+    zz = z.copy()
+    sg.check(L.gpu_host_register(zz.data.ctypes.data, zz.nbytes), "gpu_host_register")
+    for it in range(max(1, args.warmup // 2)):
+        zz.data[:] = z.data
+        mod.integrate(zz, args.duration, precision=e2e_prec, device_base=work)
+    grp.barrier()
+    e2e_times = []
+    for it in range(args.steps):
+        zz.data[:] = z.data            # fresh inputs (host side, outside the timed call)
+        t0 = time.perf_counter()
+        mod.integrate(zz, args.duration, precision=e2e_prec, device_base=work)
+        e2e_times.append(time.perf_counter() - t0)
+    grp.barrier()
+    L.gpu_host_unregister(zz.data.ctypes.data)
+    L.gpu_host_unregister(z.data.ctypes.data)
+
+    # roofline peaks measured live on this device
+    dfma = mod.probe(0)
+    ffma = mod.probe(1)
+    hbm_peak, hbm_src = measured_hbm_peak()
+
+    ms64 = float(np.mean(kern64))
+    msmx = float(np.mean(kernmx))
+    ms_step64 = grp.max(wall64 / args.steps * 1e3)
+    ms_stepmx = grp.max(wallmx / args.steps * 1e3)
+    e2e_ms = grp.max(float(np.mean(e2e_times)) * 1e3)
+    total_cells = cells * world
+    v64 = total_cells / (ms_step64 * 1e-3)
+    vmx = total_cells / (ms_stepmx * 1e-3)
+    alg_flops = steps_total * flops["total"]
+    ach64 = alg_flops / (ms64 * 1e-3) / 1e12
+    achmx = alg_flops / (msmx * 1e-3) / 1e12
+    fp64_peak = 2.0 * dfma / 1e12
+    fp32_peak = 2.0 * ffma / 1e12
+    alg_bytes = cells * hbm_bytes_per_cell(n, R)
+    head = "mixed" if args.precision == "mixed" else "f64"
+    ms_head = msmx if head == "mixed" else ms64
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_baseline(cells, args.duration, args.seed, args.cpu_seconds)
+        cpu.pop("wall_s")
+        cpu.pop("cells")
+    if rank != 0:
+        grp.close()
+        return
+    line = {
+        "metric": "cell-integrations/s",
+        "value": vmx if head == "mixed" else v64,
+        "unit": "cell-integrations/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_stepmx if head == "mixed" else ms_step64,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32+f64" if head == "mixed" else "f64",
+        "data": "synthetic",
+        "config": {"workload": f"shipped 17-species humid-air mechanism, {cells} cells x {args.duration:g} s, "
+                               f"Rodas3 rtol 1e-4 atol 1e-12 mol/L, seeded log-uniform initial states",
+                   "cells_per_gpu": cells, "duration_s": args.duration, "precision": head,
+                   "l2": "inputs larger than L2 (zone block %.0f MB per GPU)" % (block_bytes / 1e6),
+                   "kernel": "persistent work-queue kernel, autotuned launch shape",
+                   "tuning": tuned, "parallelism": f"replicas x{world} (cells partitioned, no collective)"},
+        "fp64": {"value": v64, "ms_per_step": ms_step64, "kernel_ms": ms64,
+                 "parity": "bit-identical to the reference CPU solver (tests/test_gpu_parity.py)"},
+        "mixed": {"value": vmx, "ms_per_step": ms_stepmx, "kernel_ms": msmx, "speedup_vs_fp64": v64 and vmx / v64,
+                  "rel_err_vs_fp64_max": float(rel.max()), "rel_err_vs_fp64_p99": float(np.quantile(rel, 0.99)),
+                  "rel_err_definition": "|a-b| / max(|b|, atol) per species over all cells"},
+        "steps_per_cell": {"mean": steps_total / cells, "failed_cells": failed},
+        "roofline": {"bound": "fp64", "achieved": ach64 if head == "f64" else achmx, "peak": fp64_peak,
+                     "unit": "TFLOP/s", "frac": (ach64 if head == "f64" else achmx) / fp64_peak,
+                     "traffic": None,
+                     "peak_source": "FP64 FMA throughput measured in this run (gpu_probe_throughput kind 0), x2 flops",
+                     "algorithmic_flops_per_step": flops["total"],
+                     "note": "algorithmic flops = FP64 path step count (= the oracle's) x flops per Rodas3 step; "
+                             "the mixed path does most of them in FP32",
+                     "fp64_path": {"achieved": ach64, "frac": ach64 / fp64_peak},
+                     "mixed_path": {"achieved": achmx, "frac_of_fp64_peak": achmx / fp64_peak,
+                                    "frac_of_fp32_peak": achmx / fp32_peak, "fp32_peak": fp32_peak},
+                     "hbm": {"achieved": alg_bytes / (ms_head * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                             "frac": alg_bytes / (ms_head * 1e-3) / 1e9 / hbm_peak, "peak_source": hbm_src,
+                             "algorithmic_bytes_per_cell": hbm_bytes_per_cell(n, R)}},
+        "cpu_baseline": cpu,
+        "e2e": {"value": total_cells / (e2e_ms * 1e-3), "unit": "cell-integrations/s",
+                "h2d_bytes_per_step": block_bytes, "d2h_bytes_per_step": z.mutable_rows * z.padded * 8,
+                "precision": head, "path": "gpu_copy_to_device + gpu_kin_advance + gpu_copy_to_host, pinned host block"},
+        "gpu_launches": int(lmx if head == "mixed" else l64),
+        "clocks": clk,
+    }
+    print(json.dumps(line))
+    grp.close()
+
+
+if __name__ == "__main__":
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_ours(a)

@@ -1,0 +1,254 @@
+#ifndef SIMSTACK_GPU_H
+#define SIMSTACK_GPU_H
+
+/* C ABI of the GB300 kinetics module (libsimstack_gpu.so).
+ *
+ * Drop-in for SimStack's GPU module: every export named by the reference's
+ * GPU_EXPORT_NAMES (src/gpu/gpu_api.h:112-115) is here with the reference's
+ * signature, argument meaning and error convention (0 = success, otherwise a
+ * cudaError_t value cast to int32_t), so the reference's own loader
+ * (src/platform/linux_gpu.cpp:7-31) can dlopen this library in place of its
+ * sm_86 module. The record types passed across the boundary (GpuKinLaunch,
+ * GpuInfo, KinMech, KinMethod, KinControl) have the reference's byte layout.
+ *
+ * New capability is added as extra exports, never by changing a reference
+ * signature:
+ *   - GpuKinLaunch.precision = 2: mixed precision (FP32 RHS, Jacobian and LU,
+ *     FP64 iterative-refinement residual, FP64 state and step control)
+ *   - gpu_kin_advance_queue: persistent kernel over a device work queue
+ *   - gpu_kin_autotune / gpu_kin_get_tuning: launch-shape autotuner
+ *   - kin_model_*: host-side mechanism compiler (the reference's kin_build.cpp)
+ *
+ * No torch types, no CUDA types: plain pointers and sizes. Device pointers are
+ * plain void* / double* into memory from gpu_alloc (or any CUDA allocation).
+ */
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+#define SGB_EXTERN extern "C"
+#else
+#define SGB_EXTERN extern
+#endif
+#define SGB_API SGB_EXTERN __attribute__((visibility("default")))
+
+/* --------------------------------------------------------------------------
+ * Mechanism tables: byte layout of src/sim/kinetics/kin_mech.h:22-120 at its
+ * default capacities. gpu_kin_set_mech receives this record from the caller.
+ * The capacity macros can be overridden before inclusion exactly as the
+ * reference's can; the module is built with the defaults.
+ */
+#ifndef KIN_MAX_SPECIES
+#define KIN_MAX_SPECIES 32
+#endif
+#ifndef KIN_MAX_REACTIONS
+#define KIN_MAX_REACTIONS 96
+#endif
+#define KIN_MAX_REACTANTS 3
+#define KIN_MAX_NET 6
+#ifndef KIN_MAX_NNZ
+#define KIN_MAX_NNZ 512
+#endif
+#ifndef KIN_MAX_LU_DIV
+#define KIN_MAX_LU_DIV 512
+#endif
+#ifndef KIN_MAX_LU_SUB
+#define KIN_MAX_LU_SUB 4096
+#endif
+#define KIN_MAX_STAGES 4
+#define KIN_NONE 0xFF
+
+typedef struct KinReaction {
+    uint8_t reactant[KIN_MAX_REACTANTS]; /* species index or KIN_NONE */
+    uint8_t reactant_count;
+    uint8_t net_count;
+    uint8_t net_species[KIN_MAX_NET];
+    int8_t net_coef[KIN_MAX_NET];                 /* products minus reactants */
+    uint16_t jac_index[KIN_MAX_REACTANTS][KIN_MAX_NET]; /* J scatter slot per (reactant, net entry) */
+} KinReaction;
+
+typedef struct KinLuDiv {
+    uint16_t ik, kk, sub_begin, sub_end;
+} KinLuDiv;
+typedef struct KinLuSub {
+    uint16_t ij, kj;
+} KinLuSub;
+typedef struct KinRowEntry {
+    uint16_t index;
+    uint8_t col;
+    uint8_t pad;
+} KinRowEntry;
+
+typedef struct KinMech {
+    uint32_t species_count;
+    uint32_t reaction_count;
+    KinReaction reactions[KIN_MAX_REACTIONS];
+    uint32_t nnz;
+    uint16_t diag[KIN_MAX_SPECIES];
+    uint32_t lu_div_count, lu_sub_count;
+    uint16_t div_begin[KIN_MAX_SPECIES + 1];
+    KinLuDiv lu_div[KIN_MAX_LU_DIV];
+    KinLuSub lu_sub[KIN_MAX_LU_SUB];
+    uint16_t lower_begin[KIN_MAX_SPECIES + 1];
+    uint16_t upper_begin[KIN_MAX_SPECIES + 1]; /* upper entries in DESCENDING column order */
+    KinRowEntry lower[KIN_MAX_NNZ];
+    KinRowEntry upper[KIN_MAX_NNZ];
+} KinMech;
+
+typedef struct KinMethod {
+    uint32_t stages;
+    uint32_t order;
+    double a[6], c[6];
+    double m[KIN_MAX_STAGES], e[KIN_MAX_STAGES];
+    double gamma0;
+    int32_t new_f[KIN_MAX_STAGES];
+    const char *name;
+} KinMethod;
+
+typedef struct KinControl {
+    double rtol, atol;
+    double h_min, h_max;
+    double h_start;
+    uint32_t max_steps;
+    int32_t fixed_step;
+    int32_t clamp_negative;
+} KinControl;
+
+/* --------------------------------------------------------------------------
+ * Launch records: src/gpu/gpu_api.h:30-44.
+ */
+typedef struct GpuKinLaunch {
+    double *y, *h, *steps, *rejects, *pulses, *failed;            /* solver writes */
+    double *k, *src, *pulse, *period, *pulse_first, *pulse_count; /* solver reads */
+    uint32_t padded;     /* row stride in lanes */
+    uint32_t lane_count; /* lanes [0, lane_count) are integrated; 0 = all padded lanes */
+    uint32_t precision;  /* 0 f64 lanes, 1 f32 lanes (delta form), 2 mixed FP32/FP64 (this module) */
+    double duration;     /* local time [0, duration] */
+} GpuKinLaunch;
+
+typedef struct GpuInfo {
+    char name[128];
+    uint32_t sm_major, sm_minor, multiprocessors;
+    uint64_t total_bytes, free_bytes;
+    uint64_t arena_bytes;
+} GpuInfo;
+
+#define SGB_PRECISION_F64 0u
+#define SGB_PRECISION_F32_DELTA 1u
+#define SGB_PRECISION_MIXED 2u
+
+/* --------------------------------------------------------------------------
+ * The 16 reference exports (src/gpu/gpu_api.h:46-115).
+ */
+
+/* gpu_api.h:47 -- select the device, create the module's device arena, events and
+ * non-blocking stream. */
+SGB_API int32_t gpu_init(uint32_t device_index, uint64_t arena_bytes, GpuInfo *info);
+/* gpu_api.h:50 */
+SGB_API const char *gpu_error_string(int32_t error);
+/* gpu_api.h:54 -- 256-byte aligned bump allocation from the arena; 0 when full. */
+SGB_API void *gpu_alloc(uint64_t size);
+/* gpu_api.h:57 */
+SGB_API uint64_t gpu_arena_used(void);
+/* gpu_api.h:62 -- waits for the device, then rolls the arena back to empty. */
+SGB_API void gpu_arena_reset(void);
+/* gpu_api.h:65, :68 -- copy on the module stream, then wait for it. */
+SGB_API int32_t gpu_copy_to_device(void *dst_device, const void *src_host, uint64_t size);
+SGB_API int32_t gpu_copy_to_host(void *dst_host, const void *src_device, uint64_t size);
+/* gpu_api.h:71 */
+SGB_API int32_t gpu_sync(void);
+/* gpu_api.h:75 -- the reference's particle demo kernel (kept for the loader). */
+SGB_API int32_t gpu_step_points(float *x, float *y, float *z, float *vx, float *vy, float *vz, uint32_t count, float dt);
+/* gpu_api.h:80 -- upload mechanism, method and control; cudaErrorInvalidValue when the
+ * mechanism does not fit. Selects the build-time straight-line kernels when the
+ * mechanism's FNV-1a signature matches one, else the table-driven kernels. */
+SGB_API int32_t gpu_kin_set_mech(const KinMech *mech, const KinMethod *method, const KinControl *control);
+/* gpu_api.h:85 -- advance every lane over [0, duration] and wait; kernel time in ms. */
+SGB_API int32_t gpu_kin_advance(const GpuKinLaunch *launch, float *kernel_ms);
+/* gpu_api.h:89, :91 -- page-lock a host range (already registered counts as success). */
+SGB_API int32_t gpu_host_register(void *host, uint64_t size);
+SGB_API int32_t gpu_host_unregister(void *host);
+/* gpu_api.h:99 -- upload lanes [0, lane_count) of a [rows][padded] f64 block, advance,
+ * download the first mutable_rows rows; returns without waiting. */
+SGB_API int32_t gpu_kin_advance_async(const GpuKinLaunch *launch, void *host_block, void *device_block, uint64_t rows,
+                                      uint64_t mutable_rows);
+/* gpu_api.h:105 */
+SGB_API int32_t gpu_kin_wait(float *kernel_ms, float *total_ms);
+/* gpu_api.h:109 -- 0 = one thread per cell, 1 = one warp per cell. */
+SGB_API int32_t gpu_kin_set_mode(uint32_t mode);
+
+/* --------------------------------------------------------------------------
+ * Extra exports (no reference counterpart unless cited).
+ */
+
+/* Persistent kernel: resident CTAs draw cells from a device work queue (atomic
+ * cursor in module-owned device memory), so cells with few steps do not idle
+ * warps next to stiff ones. Same results as gpu_kin_advance for every lane. */
+SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_ms);
+
+/* Launch tuning. kind: 0 static one-cell-per-thread, 1 persistent queue.
+ * block = threads per CTA (multiple of 32), chunk = cells claimed per queue
+ * pop, variant = compiled register-budget variant (0: 255 regs, 1: 128, 2: 96).
+ * gpu_kin_autotune times candidates on the given launch (which it advances
+ * repeatedly on a scratch copy it restores) and keeps the fastest. */
+typedef struct GpuKinTuning {
+    uint32_t kind, block, chunk, variant;
+    float ms;
+} GpuKinTuning;
+SGB_API int32_t gpu_kin_set_tuning(const GpuKinTuning *tuning);
+SGB_API int32_t gpu_kin_get_tuning(uint32_t precision, GpuKinTuning *tuning);
+SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuKinTuning *best);
+
+/* Kernel advances issued so far and the last one's kernel time. */
+SGB_API int32_t gpu_kin_last_stats(uint64_t *kernel_launches, float *last_kernel_ms);
+
+/* Mixed path (precision 2): iterative-refinement sweeps per stage solve, 1 (default) or 2. */
+SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps);
+
+/* Measured instruction throughput of this device, operations per second (an
+ * FMA is one operation): kind 0 FP64 FMA, 1 FP32 FMA, 2 FP32->FP64->FP32
+ * conversion pairs, 3 FP64 add, 4 FP64 reciprocal, 5 FP64 sqrt. The roofline
+ * of the integrator is reported against these. */
+SGB_API int32_t gpu_probe_throughput(uint32_t kind, double *ops_per_s);
+
+/* Device-to-device copy on the module stream; returns without waiting. */
+SGB_API int32_t gpu_copy_on_device(void *dst_device, const void *src_device, uint64_t size);
+
+/* The module's stream (a cudaStream_t), for callers ordering their own work against it. */
+SGB_API void *gpu_stream(void);
+
+/* ---------------------------------------------------------------------------
+ * Host-side mechanism compiler: src/sim/kinetics/kin_build.cpp:199-365 and
+ * air_mech.cpp:30-108, 205-276. Builds the reference-layout KinMech (same
+ * pattern, pivot order and bytes as kin_mech_finalize), rate constants and
+ * the discharge source. A handle is an opaque model.
+ */
+typedef struct KinModelHandle KinModelHandle;
+/* Rate-law kinds and parameters (kin_build.cpp:137-174):
+ *   0 Arrhenius  p = {A, n, E}           k = A (T/300)^n exp(-E/T)
+ *   1 third body p = {A, n, E}           same times [M]
+ *   2 Troe       p = {A0, n0, Ainf, ninf, fc}
+ *   3 eq-reverse p = {Keq_A, Keq_B}, ref = forward reaction index */
+SGB_API KinModelHandle *kin_model_new(void);
+SGB_API KinModelHandle *kin_model_air(void); /* the shipped 17-species humid-air mechanism, finalized */
+SGB_API void kin_model_free(KinModelHandle *model);
+SGB_API uint32_t kin_model_add_species(KinModelHandle *model, const char *name, int32_t abstract_species);
+SGB_API uint32_t kin_model_add_reaction(KinModelHandle *model, const char *equation, int32_t kind, const double *params,
+                                        int32_t ref);
+SGB_API int32_t kin_model_finalize(KinModelHandle *model); /* 0 ok, else see kin_model_error */
+SGB_API const char *kin_model_error(const KinModelHandle *model);
+/* counts[0..6] = species, reactions, nnz, lu divisions, lu updates, lower, upper */
+SGB_API void kin_model_counts(const KinModelHandle *model, uint64_t *counts);
+/* Reference-layout tables; cudaErrorInvalidValue (1) if the mechanism exceeds them. */
+SGB_API int32_t kin_model_kinmech(const KinModelHandle *model, KinMech *out);
+SGB_API uint64_t kin_mech_signature(const KinMech *mech); /* FNV-1a over the record */
+SGB_API void kin_model_rate_constants(const KinModelHandle *model, double T, double M, double *k);
+/* Rate constants for `cells` cells of a [reactions][padded] block from T and M per cell. */
+SGB_API void kin_model_rate_block(const KinModelHandle *model, const double *T, const double *M, uint32_t cells,
+                                  uint32_t padded, double *k);
+SGB_API KinMethod kin_method_coefficients(uint32_t method_id); /* 0 ros2, 1 ros3, 2 rodas3 */
+/* Averaged-discharge source per second for the shipped mechanism (air_mech.cpp:205-276). */
+SGB_API void kin_air_source_delta(const double *y, uint32_t species, double energy_J_cm3, double T_K, double *delta);
+
+#endif /* SIMSTACK_GPU_H */

@@ -1,0 +1,374 @@
+"""TEST INFRASTRUCTURE -- NOT PART OF THE PRODUCT.
+
+ctypes bindings for the CPU oracle (``liboracle.so``, built from
+``kin_oracle.cpp``) and, where it was built, for the reference's own CPU solver
+(``_ref/libref.so`` and ``_ref/libref_big.so``, compiled from the reference
+sources by ``oracle/Makefile``). Imported only by ``tests/``,
+``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py``.
+
+Zone blocks are passed as the reference's SoA layout (``src/sim/dbd.cpp:40-58``):
+``y[species][padded]``, ``h``, ``steps``, ``rejects``, ``pulses``, ``failed``,
+``k[reaction][padded]``, ``src[species][padded]``, ``pulse[species][padded]``,
+``period``, ``pulse_first``, ``pulse_count`` -- a dict of float64 numpy arrays.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+REF_LIB = os.path.join(HERE, "_ref", "libref.so")
+REF_BIG_LIB = os.path.join(HERE, "_ref", "libref_big.so")
+KINMECH_BYTES = 30044
+
+METHOD_IDS = {"ros2": 0, "ros3": 1, "rodas3": 2}
+RATE_KIND = {"arr": 0, "m": 1, "troe": 2, "eqrev": 3}
+
+
+class Control(C.Structure):
+    """KinControl (src/sim/kinetics/kin_mech.h:112-120)."""
+
+    _fields_ = [("rtol", C.c_double), ("atol", C.c_double), ("h_min", C.c_double), ("h_max", C.c_double),
+                ("h_start", C.c_double), ("max_steps", C.c_uint32), ("fixed_step", C.c_int32),
+                ("clamp_negative", C.c_int32)]
+
+
+class LaneArrays(C.Structure):
+    """DbdLaneArrays (src/sim/dbd_lanes.h:13-19)."""
+
+    _fields_ = [(n, C.c_void_p) for n in ("y", "h", "steps", "rejects", "pulses", "failed", "k", "src", "pulse",
+                                          "period", "pulse_first", "pulse_count")] + [("padded", C.c_uint32)]
+
+
+BLOCK_FIELDS = ("y", "h", "steps", "rejects", "pulses", "failed", "k", "src", "pulse", "period", "pulse_first",
+                "pulse_count")
+
+
+def aligned_zeros(shape, align: int = 64) -> np.ndarray:
+    """float64 zeros whose data pointer is `align`-byte aligned (the reference's
+    f64x4 lanes use aligned AVX loads; SoaPush aligns to 64 bytes)."""
+    count = int(np.prod(shape))
+    raw = np.zeros(count + align // 8, np.float64)
+    off = (-raw.ctypes.data % align) // 8
+    return raw[off:off + count].reshape(shape)
+
+
+def lane_arrays(block: dict, padded: int) -> LaneArrays:
+    la = LaneArrays()
+    for name in BLOCK_FIELDS:
+        arr = block[name]
+        assert arr.dtype == np.float64 and arr.flags["C_CONTIGUOUS"], name
+        setattr(la, name, arr.ctypes.data)
+    la.padded = padded
+    return la
+
+
+def control(rtol=1e-4, atol=6.02214076e8, h_min=1e-14, h_max=0.0, h_start=1e-9, max_steps=1_000_000,
+            fixed_step=0, clamp_negative=1) -> Control:
+    return Control(rtol, atol, h_min, h_max, h_start, max_steps, fixed_step, clamp_negative)
+
+
+def build(quiet: bool = True) -> None:
+    """Compile liboracle.so with the oracle's Makefile (any host)."""
+    out = subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], capture_output=True, text=True)
+    if out.returncode != 0:
+        raise RuntimeError("oracle build failed:\n" + out.stdout + out.stderr)
+
+
+_lib = None
+
+
+def lib() -> C.CDLL:
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        L = C.CDLL(LIB)
+        vp, u32, i32, d, u64 = C.c_void_p, C.c_uint32, C.c_int32, C.c_double, C.c_uint64
+        L.or_mech_new.restype = vp
+        L.or_mech_new_air.restype = vp
+        L.or_mech_free.argtypes = [vp]
+        L.or_add_species.argtypes = [vp, C.c_char_p, i32]
+        L.or_add_species.restype = u32
+        L.or_add_reaction.argtypes = [vp, C.c_char_p, i32, C.POINTER(d), i32]
+        L.or_add_reaction.restype = u32
+        L.or_finalize.argtypes = [vp]
+        L.or_error.argtypes = [vp]
+        L.or_error.restype = C.c_char_p
+        L.or_counts.argtypes = [vp, C.POINTER(u64)]
+        L.or_export_kinmech.argtypes = [vp, vp, C.POINTER(u64)]
+        L.or_export_kinmech.restype = i32
+        L.or_pattern.argtypes = [vp, vp]
+        L.or_lu_ops.argtypes = [vp, vp, vp]
+        L.or_rate_constants.argtypes = [vp, d, d, vp]
+        L.or_fun.argtypes = [vp, vp, vp, vp, vp]
+        L.or_jac.argtypes = [vp, vp, vp, vp]
+        L.or_decomp_solve.argtypes = [vp, vp, d, vp, vp]
+        L.or_integrate_f64.argtypes = [vp, i32, C.POINTER(Control), vp, vp, vp, C.POINTER(d), d, C.POINTER(d), vp]
+        L.or_integrate_f64.restype = i32
+        L.or_advance.argtypes = [vp, i32, C.POINTER(Control), C.POINTER(LaneArrays), u32, u32, d, u32, u32]
+        L.or_advance.restype = i32
+        L.or_source_delta.argtypes = [vp, u32, d, d, vp]
+        L.or_advect.argtypes = [vp, u32, u32, u32, vp, d, u32]
+        L.or_fnv1a.argtypes = [vp, u64]
+        L.or_fnv1a.restype = u64
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray) -> int:
+    return a.ctypes.data
+
+
+class Mechanism:
+    """A mechanism in the oracle's wide-index tables."""
+
+    def __init__(self, handle=None):
+        self.h = handle if handle is not None else lib().or_mech_new()
+
+    @classmethod
+    def air(cls) -> "Mechanism":
+        return cls(lib().or_mech_new_air())
+
+    def __del__(self):
+        if getattr(self, "h", None) and _lib is not None:
+            _lib.or_mech_free(self.h)
+            self.h = None
+
+    def add_species(self, name: str, abstract: bool = False) -> int:
+        return lib().or_add_species(self.h, name.encode(), int(abstract))
+
+    def add_reaction(self, equation: str, kind: str = "arr", params=(1.0, 0.0, 0.0), ref: int = 0) -> int:
+        p = (C.c_double * 5)(*(list(params) + [0.0] * (5 - len(params))))
+        return lib().or_add_reaction(self.h, equation.encode(), RATE_KIND[kind], p, ref)
+
+    def finalize(self) -> None:
+        lib().or_finalize(self.h)
+
+    @property
+    def error(self) -> str:
+        return lib().or_error(self.h).decode()
+
+    def counts(self) -> dict:
+        c = (C.c_uint64 * 8)()
+        lib().or_counts(self.h, c)
+        keys = ("n", "R", "nnz", "pivots", "updates", "lower", "upper", "failed")
+        return dict(zip(keys, [int(v) for v in c]))
+
+    def kinmech(self):
+        """(bytes, fnv1a) of the reference-layout KinMech, or (None, None) if it does not fit."""
+        buf = np.zeros(KINMECH_BYTES, np.uint8)
+        sig = C.c_uint64()
+        ok = lib().or_export_kinmech(self.h, _ptr(buf), C.byref(sig))
+        return (buf.tobytes(), int(sig.value)) if ok else (None, None)
+
+    def pattern(self) -> np.ndarray:
+        n = self.counts()["n"]
+        out = np.zeros(n * n, np.uint8)
+        lib().or_pattern(self.h, _ptr(out))
+        return out.reshape(n, n)
+
+    def lu_ops(self):
+        c = self.counts()
+        piv = np.zeros((max(c["pivots"], 1), 4), np.uint32)
+        upd = np.zeros((max(c["updates"], 1), 2), np.uint32)
+        lib().or_lu_ops(self.h, _ptr(piv), _ptr(upd))
+        return piv[: c["pivots"]], upd[: c["updates"]]
+
+    def rate_constants(self, T: float, M: float) -> np.ndarray:
+        k = np.zeros(max(self.counts()["R"], 1))
+        lib().or_rate_constants(self.h, T, M, _ptr(k))
+        return k[: self.counts()["R"]]
+
+    def fun(self, k, src, y) -> np.ndarray:
+        f = np.zeros(len(y))
+        lib().or_fun(self.h, _ptr(np.ascontiguousarray(k, np.float64)), _ptr(np.ascontiguousarray(src, np.float64)),
+                     _ptr(np.ascontiguousarray(y, np.float64)), _ptr(f))
+        return f
+
+    def jac(self, k, y) -> np.ndarray:
+        out = np.zeros(self.counts()["nnz"])
+        lib().or_jac(self.h, _ptr(np.ascontiguousarray(k, np.float64)), _ptr(np.ascontiguousarray(y, np.float64)), _ptr(out))
+        return out
+
+    def decomp_solve(self, jac, ghinv, b):
+        x = np.array(b, np.float64)
+        lu = np.zeros(self.counts()["nnz"])
+        lib().or_decomp_solve(self.h, _ptr(np.ascontiguousarray(jac, np.float64)), ghinv, _ptr(x), _ptr(lu))
+        return x, lu
+
+    def integrate(self, method: str, ctl: Control, k, src, y0, t_end: float, h0: float = 0.0):
+        y = np.array(y0, np.float64)
+        t = C.c_double(0.0)
+        h = C.c_double(h0)
+        stats = np.zeros(4)
+        lib().or_integrate_f64(self.h, METHOD_IDS[method], C.byref(ctl), _ptr(np.ascontiguousarray(k, np.float64)),
+                               _ptr(np.ascontiguousarray(src, np.float64)), _ptr(y), C.byref(t), t_end, C.byref(h),
+                               _ptr(stats))
+        return y, t.value, h.value, stats
+
+    def advance(self, method: str, ctl: Control, block: dict, padded: int, begin: int, end: int, duration: float,
+                precision: int = 0, threads: int = 0) -> None:
+        la = lane_arrays(block, padded)
+        rc = lib().or_advance(self.h, METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, precision,
+                              threads)
+        if rc != 0:
+            raise RuntimeError(f"or_advance failed: {rc}")
+
+
+def source_delta(y: np.ndarray, energy_J_cm3: float, T_K: float) -> np.ndarray:
+    y = np.ascontiguousarray(y, np.float64)
+    out = np.zeros(len(y))
+    lib().or_source_delta(_ptr(y), len(y), energy_J_cm3, T_K, _ptr(out))
+    return out
+
+
+def advect(x: np.ndarray, inlet: np.ndarray, courant: float, substeps: int) -> None:
+    """In place on a C-contiguous [species][cells] float64 block."""
+    assert x.flags["C_CONTIGUOUS"] and x.dtype == np.float64
+    inlet = np.ascontiguousarray(inlet, np.float64)
+    lib().or_advect(_ptr(x), x.shape[0], x.shape[1], x.shape[1], _ptr(inlet), courant, substeps)
+
+
+def fnv1a(data: bytes) -> int:
+    buf = np.frombuffer(data, np.uint8).copy()
+    return int(lib().or_fnv1a(_ptr(buf), len(buf)))
+
+
+# ---------------------------------------------------------------------------
+# The reference's own CPU solver (only where oracle/_ref was built).
+
+_ref = None
+_ref_big = None
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_LIB)
+
+
+def ref() -> C.CDLL:
+    global _ref
+    if _ref is None:
+        L = C.CDLL(REF_LIB)
+        vp, u32, i32, d, u64 = C.c_void_p, C.c_uint32, C.c_int32, C.c_double, C.c_uint64
+        L.ref_kinmech_size.restype = u64
+        L.ref_air_kinmech.argtypes = [vp, C.POINTER(u64), C.POINTER(u64)]
+        L.ref_air_kinmech.restype = i32
+        L.ref_air_rate_constants.argtypes = [d, d, vp]
+        L.ref_air_source_delta.argtypes = [vp, d, d, vp]
+        L.ref_air_advance.argtypes = [i32, C.POINTER(Control), C.POINTER(LaneArrays), u32, u32, d, i32]
+        L.ref_air_advance.restype = i32
+        L.ref_robertson.argtypes = [i32, C.POINTER(Control), d, vp, vp]
+        L.ref_robertson.restype = i32
+        _ref = L
+    return _ref
+
+
+def ref_air_kinmech():
+    buf = np.zeros(KINMECH_BYTES, np.uint8)
+    sig, gen = C.c_uint64(), C.c_uint64()
+    assert ref().ref_air_kinmech(_ptr(buf), C.byref(sig), C.byref(gen)) == 1
+    return buf.tobytes(), int(sig.value), int(gen.value)
+
+
+def ref_air_rate_constants(T: float, M: float, R: int = 44) -> np.ndarray:
+    k = np.zeros(R)
+    ref().ref_air_rate_constants(T, M, _ptr(k))
+    return k
+
+
+def ref_air_source_delta(y, energy_J_cm3, T_K) -> np.ndarray:
+    y = np.ascontiguousarray(y, np.float64)
+    out = np.zeros(len(y))
+    ref().ref_air_source_delta(_ptr(y), energy_J_cm3, T_K, _ptr(out))
+    return out
+
+
+REF_VARIANTS = {"f64x4_gen": 0, "f64x4_table": 1, "f64_table": 2, "f32x8_gen": 3, "f32_gen": 4}
+
+
+def ref_air_advance(method: str, ctl: Control, block: dict, padded: int, begin: int, end: int, duration: float,
+                    variant: str = "f64x4_gen") -> None:
+    la = lane_arrays(block, padded)
+    rc = ref().ref_air_advance(METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, REF_VARIANTS[variant])
+    if rc != 0:
+        raise RuntimeError(f"ref_air_advance: {rc}")
+
+
+def ref_robertson(method: str, ctl: Control, t_end: float = 40.0):
+    y = np.array([1.0, 0.0, 0.0])
+    stats = np.zeros(4)
+    ref().ref_robertson(METHOD_IDS[method], C.byref(ctl), t_end, _ptr(y), _ptr(stats))
+    return y, stats
+
+
+class RefBigMechanism:
+    """The reference's builder with larger KIN_MAX_* capacities (u16 tables)."""
+
+    def __init__(self):
+        global _ref_big
+        if _ref_big is None:
+            L = C.CDLL(REF_BIG_LIB)
+            vp, u32, i32, d, u64 = C.c_void_p, C.c_uint32, C.c_int32, C.c_double, C.c_uint64
+            L.ref_big_new.restype = vp
+            L.ref_big_free.argtypes = [vp]
+            L.ref_big_add_species.argtypes = [vp, C.c_char_p, i32]
+            L.ref_big_add_reaction.argtypes = [vp, C.c_char_p, i32, C.POINTER(d), i32]
+            L.ref_big_finalize.argtypes = [vp]
+            L.ref_big_error.argtypes = [vp]
+            L.ref_big_error.restype = C.c_char_p
+            L.ref_big_counts.argtypes = [vp, C.POINTER(u64)]
+            L.ref_big_lu_ops.argtypes = [vp, vp, vp]
+            L.ref_big_rate_constants.argtypes = [vp, d, d, vp]
+            L.ref_big_advance.argtypes = [vp, i32, C.POINTER(Control), C.POINTER(LaneArrays), u32, u32, d, i32]
+            L.ref_big_advance.restype = i32
+            _ref_big = L
+        self.L = _ref_big
+        self.h = self.L.ref_big_new()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.L.ref_big_free(self.h)
+            self.h = None
+
+    def add_species(self, name, abstract=False):
+        return self.L.ref_big_add_species(self.h, name.encode(), int(abstract))
+
+    def add_reaction(self, equation, kind="arr", params=(1.0, 0.0, 0.0), ref=0):
+        p = (C.c_double * 5)(*(list(params) + [0.0] * (5 - len(params))))
+        return self.L.ref_big_add_reaction(self.h, equation.encode(), RATE_KIND[kind], p, ref)
+
+    def finalize(self):
+        self.L.ref_big_finalize(self.h)
+
+    @property
+    def error(self):
+        return self.L.ref_big_error(self.h).decode()
+
+    def counts(self):
+        c = (C.c_uint64 * 8)()
+        self.L.ref_big_counts(self.h, c)
+        return dict(zip(("n", "R", "nnz", "pivots", "updates", "lower", "upper", "failed"), [int(v) for v in c]))
+
+    def lu_ops(self):
+        c = self.counts()
+        piv = np.zeros((max(c["pivots"], 1), 4), np.uint32)
+        upd = np.zeros((max(c["updates"], 1), 2), np.uint32)
+        self.L.ref_big_lu_ops(self.h, _ptr(piv), _ptr(upd))
+        return piv[: c["pivots"]], upd[: c["updates"]]
+
+    def rate_constants(self, T, M):
+        R = self.counts()["R"]
+        k = np.zeros(max(R, 1))
+        self.L.ref_big_rate_constants(self.h, T, M, _ptr(k))
+        return k[:R]
+
+    def advance(self, method, ctl, block, padded, begin, end, duration, variant=0):
+        la = lane_arrays(block, padded)
+        rc = self.L.ref_big_advance(self.h, METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, variant)
+        if rc != 0:
+            raise RuntimeError(f"ref_big_advance: {rc}")

@@ -1,0 +1,129 @@
+// TEST INFRASTRUCTURE -- NOT PART OF THE PRODUCT.
+//
+// Thin C ABI over the reference's own CPU solver, compiled from the reference
+// sources where they lie (include path REF_DIR/src, nothing copied) by
+// oracle/Makefile into oracle/_ref/. The tests use it here to pin the oracle
+// restatement (kin_oracle.cpp) bit for bit and to generate tests/golden/.
+// It is never built on a machine without the reference sources.
+//
+// What it calls: kin_mech_finalize and air_mech_build (kin_build.cpp,
+// air_mech.cpp), kin_eval_rate_constants, kin_integrate (kin_solver.h),
+// dbd_advance_cpu / dbd_advance_group (dbd.cpp, dbd_lanes.h) with the
+// generated AirGenOps or the table walk, f64 / f64x4 / f32 / f32x8 lanes,
+// and air_source_delta.
+
+// Profiler shim: the reference's base_debug.h reads the x86 TSC; the solver
+// only uses its TIMED_FUNCTION() markers, which compile to nothing here.
+#define BASE_DEBUG_H
+#define TIMED_BLOCK(name)
+#define TIMED_FUNCTION()
+struct DebugTable;
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <math.h>
+
+#include "sim_platform.h"
+#include "sim/dbd.cpp"
+
+#define REF_API extern "C" __attribute__((visibility("default")))
+
+static KinModel g_air;
+static AirSpecies g_air_sp;
+static int g_air_built;
+
+static KinModel *air_model() {
+    if (!g_air_built) {
+        air_mech_build(&g_air, &g_air_sp);
+        g_air_built = 1;
+    }
+    return &g_air;
+}
+
+REF_API u64 ref_kinmech_size(void) { return sizeof(KinMech); }
+
+// The shipped mechanism's KinMech bytes, and the generated kernels' signature.
+REF_API s32 ref_air_kinmech(void *out, u64 *signature, u64 *generated_signature) {
+    KinModel *m = air_model();
+    if (m->error) return 0;
+    memcpy(out, &m->mech, sizeof(KinMech));
+    if (signature) *signature = hash_fnv1a_64(&m->mech, sizeof(KinMech));
+    if (generated_signature) *generated_signature = AirGenOps::signature;
+    return 1;
+}
+
+REF_API void ref_air_rate_constants(f64 T, f64 M, f64 *k) { kin_eval_rate_constants(air_model(), T, M, k); }
+
+REF_API void ref_air_source_delta(const f64 *y, f64 energy_J_cm3, f64 T_K, f64 *delta) {
+    AirSourceModel src = air_source_defaults();
+    air_source_delta(&g_air_sp, &src, y, air_model()->mech.species_count, energy_J_cm3, delta, T_K);
+}
+
+struct RefControl {
+    f64 rtol, atol, h_min, h_max, h_start;
+    u32 max_steps;
+    s32 fixed_step, clamp_negative;
+};
+
+static KinControl to_control(const RefControl *c) {
+    KinControl k = {};
+    k.rtol = c->rtol; k.atol = c->atol; k.h_min = c->h_min; k.h_max = c->h_max; k.h_start = c->h_start;
+    k.max_steps = c->max_steps; k.fixed_step = c->fixed_step; k.clamp_negative = c->clamp_negative;
+    return k;
+}
+
+struct RefLaneArrays {
+    f64 *y, *h, *steps, *rejects, *pulses, *failed;
+    const f64 *k, *src, *pulse, *period, *pulse_first, *pulse_count;
+    u32 padded;
+};
+
+// Lanes [first, end) of a zone block with the shipped mechanism.
+// variant 0: f64x4 generated (the production CPU path), 1: f64x4 table walk,
+// 2: f64 scalar table walk, 3: f32x8 generated (Delta), 4: f32 scalar generated (Delta).
+REF_API s32 ref_air_advance(s32 method_id, const RefControl *rc, const RefLaneArrays *a, u32 first, u32 end,
+                            f64 duration, s32 variant) {
+    KinModel *model = air_model();
+    KinMethod method = kin_method((KinMethodId)method_id);
+    KinControl ctl = to_control(rc);
+    DbdZones z = {};
+    z.padded = a->padded;
+    z.n_species = model->mech.species_count;
+    z.n_reactions = model->mech.reaction_count;
+    z.y = a->y; z.h = a->h; z.steps = a->steps; z.rejects = a->rejects; z.pulses = a->pulses; z.failed = a->failed;
+    z.k = (f64 *)a->k; z.src = (f64 *)a->src; z.pulse = (f64 *)a->pulse; z.period = (f64 *)a->period;
+    z.pulse_first = (f64 *)a->pulse_first; z.pulse_count = (f64 *)a->pulse_count;
+    if ((variant == 0 || variant == 1) && (first % 4 || end % 4)) return -1;
+    if (variant == 3 && (first % 8 || end % 8)) return -1;
+    switch (variant) {
+        case 0: dbd_advance_cpu<f64x4, AirGenOps>(&z, &model->mech, &method, &ctl, duration, first, end); break;
+        case 1: dbd_advance_cpu<f64x4>(&z, &model->mech, &method, &ctl, duration, first, end); break;
+        case 2: dbd_advance_cpu<f64>(&z, &model->mech, &method, &ctl, duration, first, end); break;
+        case 3: dbd_advance_cpu<f32x8, AirGenOps, true>(&z, &model->mech, &method, &ctl, duration, first, end); break;
+        case 4: dbd_advance_cpu<f32, AirGenOps, true>(&z, &model->mech, &method, &ctl, duration, first, end); break;
+        default: return -1;
+    }
+    return 0;
+}
+
+// Robertson (test_kinetics.cpp:151-180 set-up): one scalar integration.
+REF_API s32 ref_robertson(s32 method_id, const RefControl *rc, f64 t_end, f64 *y3, f64 *stats4) {
+    KinModel *model = (KinModel *)calloc(1, sizeof(KinModel));
+    kin_add_species(model, "A", 1);
+    kin_add_species(model, "B", 1);
+    kin_add_species(model, "C", 1);
+    kin_add_reaction(model, "A -> B", kin_arr(0.04));
+    kin_add_reaction(model, "B + B -> C + B", kin_arr(3.0e7));
+    kin_add_reaction(model, "B + C -> A + C", kin_arr(1.0e4));
+    kin_mech_finalize(model);
+    f64 k[3];
+    kin_eval_rate_constants(model, 300.0, 1.0, k);
+    KinMethod method = kin_method((KinMethodId)method_id);
+    KinControl ctl = to_control(rc);
+    f64 src[3] = {}, t = 0.0, h = 0.0;
+    KinLaneStats<f64> st = {};
+    kin_integrate(&model->mech, &method, &ctl, k, src, y3, t, t_end, h, st);
+    stats4[0] = st.steps; stats4[1] = st.rejects; stats4[2] = st.pulses; stats4[3] = st.failed;
+    free(model);
+    return 0;
+}

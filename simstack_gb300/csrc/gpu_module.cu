@@ -1,0 +1,504 @@
+// Exports of the GB300 kinetics module: the reference's 16-entry GPU C ABI
+// (src/gpu/gpu_api.h) plus the module's extra entry points. One device, one
+// module-owned non-blocking stream; every copy and kernel of the module is
+// ordered on it (the reference's rule, src/gpu/kernels.cu:333-348).
+
+#include <cuda_runtime.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "../../include/simstack_gpu.h"
+#include "kin_kernels.cuh"
+#include "kin_table.cuh"
+#include "mech.h"
+
+namespace sgb {
+cudaError_t launch_air_p0(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t launch_air_p1(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t launch_air_p2(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_air_p0(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t occupancy_air_p1(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t occupancy_air_p2(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t launch_table_p0(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t launch_table_p1(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t launch_table_p2(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_table_p0(uint32_t, uint32_t, size_t, int *);
+cudaError_t occupancy_table_p1(uint32_t, uint32_t, size_t, int *);
+cudaError_t occupancy_table_p2(uint32_t, uint32_t, size_t, int *);
+uint64_t air_ops_signature();
+cudaError_t run_probe(uint32_t kind, int sms, cudaStream_t stream, double *ops_per_s);
+}   // namespace sgb
+
+using namespace sgb;
+
+namespace {
+
+struct Module {
+    bool ready = false;
+    int device = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t kin_start = nullptr, kin_stop = nullptr, async_begin = nullptr, async_end = nullptr;
+    uint8_t *arena = nullptr;
+    uint64_t arena_size = 0, arena_used = 0;
+    // mechanism
+    bool have_mech = false, generated = false;
+    KinMech mech;
+    KinMethod method;
+    KinControl control;
+    void *d_tables = nullptr;      // KinMech image, kTableBytes
+    uint32_t *d_cursor = nullptr;  // work-queue cursor
+    uint32_t *d_error = nullptr;   // bounded-wait error flag
+    uint32_t mode = 0;
+    GpuKinTuning tuning[3];
+    uint32_t ir_sweeps = 1;
+    uint64_t launches = 0;
+    float last_ms = 0.0f;
+};
+Module g;
+
+const GpuKinTuning kDefaultTuning = {1u, 128u, 1u, 0u, 0.0f};
+
+bool is_rodas3(const KinMethod *m) {
+    KinMethod r = method_coefficients(2);
+    return m->stages == r.stages && m->order == r.order && memcmp(m->a, r.a, sizeof(r.a)) == 0 &&
+           memcmp(m->c, r.c, sizeof(r.c)) == 0 && memcmp(m->m, r.m, sizeof(r.m)) == 0 &&
+           memcmp(m->e, r.e, sizeof(r.e)) == 0 && m->gamma0 == r.gamma0 && memcmp(m->new_f, r.new_f, sizeof(r.new_f)) == 0;
+}
+
+void fill_args(const GpuKinLaunch *L, DevArgs *A) {
+    memset(A, 0, sizeof(*A));
+    A->y = L->y; A->h = L->h; A->steps = L->steps; A->rejects = L->rejects; A->pulses = L->pulses; A->failed = L->failed;
+    A->k = L->k; A->src = L->src; A->pulse = L->pulse; A->period = L->period;
+    A->pulse_first = L->pulse_first; A->pulse_count = L->pulse_count;
+    A->padded = L->padded;
+    A->lanes = L->lane_count ? L->lane_count : L->padded;
+    A->duration = L->duration;
+    A->ctl = g.control;
+    memcpy(A->ma, g.method.a, sizeof(A->ma));
+    memcpy(A->mc, g.method.c, sizeof(A->mc));
+    memcpy(A->mm, g.method.m, sizeof(A->mm));
+    memcpy(A->me, g.method.e, sizeof(A->me));
+    A->gamma0 = g.method.gamma0;
+    memcpy(A->new_f, g.method.new_f, sizeof(A->new_f));
+    A->stages = g.method.stages;
+    A->order = g.method.order;
+    A->ir_sweeps = g.ir_sweeps;
+    A->cursor = g.d_cursor;
+    A->error_flag = g.d_error;
+    A->tables = g.d_tables;
+    A->table_bytes = kTableBytes;
+}
+
+cudaError_t occupancy(uint32_t prec, const GpuKinTuning &t, int *blocks) {
+    if (g.generated) {
+        if (prec == 0) return occupancy_air_p0(t.kind, t.variant, t.block, blocks);
+        if (prec == 1) return occupancy_air_p1(t.kind, t.variant, t.block, blocks);
+        return occupancy_air_p2(t.kind, t.variant, t.block, blocks);
+    }
+    if (prec == 0) return occupancy_table_p0(t.kind, t.block, kTableBytes, blocks);
+    if (prec == 1) return occupancy_table_p1(t.kind, t.block, kTableBytes, blocks);
+    return occupancy_table_p2(t.kind, t.block, kTableBytes, blocks);
+}
+
+// Launches one advance of `A` with tuning `t` on the module stream.
+cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &A) {
+    if (A.lanes == 0) return cudaSuccess;
+    Shape s;
+    s.kind = t.kind;
+    s.block = t.block;
+    s.variant = t.variant;
+    s.smem = g.generated ? 0 : kTableBytes;
+    if (t.kind == 0) {
+        s.grid = (A.lanes + t.block - 1) / t.block;
+    } else {
+        int per_sm = 0;
+        cudaError_t e = occupancy(prec, t, &per_sm);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+        uint32_t resident = (uint32_t)per_sm * (uint32_t)g.sms;
+        uint32_t needed = (A.lanes + t.block - 1) / t.block;
+        s.grid = resident < needed ? resident : needed;
+        e = cudaMemsetAsync(g.d_cursor, 0, sizeof(uint32_t), g.stream);
+        if (e != cudaSuccess) return e;
+    }
+    if (g.generated) {
+        if (prec == 0) return launch_air_p0(s, A, g.stream);
+        if (prec == 1) return launch_air_p1(s, A, g.stream);
+        return launch_air_p2(s, A, g.stream);
+    }
+    s.variant = 0;
+    if (prec == 0) return launch_table_p0(s, A, g.stream);
+    if (prec == 1) return launch_table_p1(s, A, g.stream);
+    return launch_table_p2(s, A, g.stream);
+}
+
+cudaError_t check_launch(const GpuKinLaunch *L) {
+    if (!g.ready) return cudaErrorInitializationError;
+    if (!g.have_mech) return cudaErrorInvalidValue;
+    if (!L || L->precision > 2 || L->padded == 0) return cudaErrorInvalidValue;
+    if (L->lane_count > L->padded) return cudaErrorInvalidValue;
+    if (!L->y || !L->h || !L->steps || !L->rejects || !L->pulses || !L->failed || !L->k || !L->src || !L->pulse ||
+        !L->period || !L->pulse_first || !L->pulse_count)
+        return cudaErrorInvalidValue;
+    return cudaSuccess;
+}
+
+cudaError_t read_error_flag() {
+    uint32_t flag = 0;
+    cudaError_t e = cudaMemcpyAsync(&flag, g.d_error, sizeof(flag), cudaMemcpyDeviceToHost, g.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
+    if (e != cudaSuccess) return e;
+    if (flag) {
+        cudaMemsetAsync(g.d_error, 0, sizeof(uint32_t), g.stream);
+        cudaStreamSynchronize(g.stream);
+        return cudaErrorTimeout;
+    }
+    return cudaSuccess;
+}
+
+// Timed advance on the module stream; waits for completion.
+cudaError_t advance_sync(const GpuKinLaunch *L, const GpuKinTuning &t, float *kernel_ms) {
+    cudaError_t e = check_launch(L);
+    if (e != cudaSuccess) return e;
+    DevArgs A;
+    fill_args(L, &A);
+    cudaEventRecord(g.kin_start, g.stream);
+    e = launch_advance(L->precision, t, A);
+    cudaEventRecord(g.kin_stop, g.stream);
+    if (e != cudaSuccess) return e;
+    e = cudaEventSynchronize(g.kin_stop);
+    if (e != cudaSuccess) return e;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, g.kin_start, g.kin_stop);
+    g.last_ms = ms;
+    ++g.launches;
+    if (kernel_ms) *kernel_ms = ms;
+    e = read_error_flag();
+    if (e != cudaSuccess) return e;
+    return cudaGetLastError();
+}
+
+}   // namespace
+
+// ===========================================================================
+// The reference's exports (src/gpu/gpu_api.h:46-115).
+
+SGB_API int32_t gpu_init(uint32_t device_index, uint64_t arena_bytes, GpuInfo *info) {
+    memset(info, 0, sizeof(*info));
+    cudaError_t e = cudaSetDevice((int)device_index);
+    if (e != cudaSuccess) return (int32_t)e;
+    cudaDeviceProp prop;
+    e = cudaGetDeviceProperties(&prop, (int)device_index);
+    if (e != cudaSuccess) return (int32_t)e;
+    snprintf(info->name, sizeof(info->name), "%s", prop.name);
+    info->sm_major = (uint32_t)prop.major;
+    info->sm_minor = (uint32_t)prop.minor;
+    info->multiprocessors = (uint32_t)prop.multiProcessorCount;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    info->free_bytes = free_b;
+    info->total_bytes = total_b;
+    if (g.ready) {   // re-init: release the previous arena and scratch
+        cudaDeviceSynchronize();
+        cudaFree(g.arena);
+        cudaFree(g.d_tables);
+        cudaFree(g.d_cursor);
+        g.arena = nullptr;
+        g.d_tables = nullptr;
+        g.d_cursor = nullptr;
+        g.ready = false;
+    }
+    void *base = nullptr;
+    if (arena_bytes) {
+        e = cudaMalloc(&base, arena_bytes);
+        if (e != cudaSuccess) return (int32_t)e;
+    }
+    g.arena = (uint8_t *)base;
+    g.arena_size = arena_bytes;
+    g.arena_used = 0;
+    info->arena_bytes = arena_bytes;
+    e = cudaMalloc(&g.d_tables, kTableBytes);
+    if (e != cudaSuccess) return (int32_t)e;
+    e = cudaMalloc((void **)&g.d_cursor, 256);   // cursor at +0, error flag at +128
+    if (e != cudaSuccess) return (int32_t)e;
+    g.d_error = (uint32_t *)((uint8_t *)g.d_cursor + 128);
+    cudaMemset(g.d_cursor, 0, 256);
+    if (!g.stream) {
+        cudaEventCreate(&g.kin_start);
+        cudaEventCreate(&g.kin_stop);
+        cudaEventCreate(&g.async_begin);
+        cudaEventCreate(&g.async_end);
+        cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
+    }
+    g.device = (int)device_index;
+    g.sms = prop.multiProcessorCount;
+    for (int p = 0; p < 3; ++p) g.tuning[p] = kDefaultTuning;
+    g.have_mech = false;
+    g.ready = true;
+    return (int32_t)cudaGetLastError();
+}
+
+SGB_API const char *gpu_error_string(int32_t error) { return cudaGetErrorString((cudaError_t)error); }
+
+SGB_API void *gpu_alloc(uint64_t size) {
+    uint64_t aligned = (size + 255) & ~255ull;
+    if (!g.arena || g.arena_used + aligned > g.arena_size) return nullptr;
+    void *p = g.arena + g.arena_used;
+    g.arena_used += aligned;
+    return p;
+}
+
+SGB_API uint64_t gpu_arena_used(void) { return g.arena_used; }
+
+SGB_API void gpu_arena_reset(void) {
+    cudaDeviceSynchronize();
+    g.arena_used = 0;
+}
+
+SGB_API int32_t gpu_copy_to_device(void *dst_device, const void *src_host, uint64_t size) {
+    cudaError_t e = cudaMemcpyAsync(dst_device, src_host, size, cudaMemcpyHostToDevice, g.stream);
+    if (e != cudaSuccess) return (int32_t)e;
+    return (int32_t)cudaStreamSynchronize(g.stream);
+}
+
+SGB_API int32_t gpu_copy_to_host(void *dst_host, const void *src_device, uint64_t size) {
+    cudaError_t e = cudaMemcpyAsync(dst_host, src_device, size, cudaMemcpyDeviceToHost, g.stream);
+    if (e != cudaSuccess) return (int32_t)e;
+    return (int32_t)cudaStreamSynchronize(g.stream);
+}
+
+SGB_API int32_t gpu_sync(void) { return (int32_t)cudaStreamSynchronize(g.stream); }
+
+namespace {
+__global__ void step_points_kernel(float *x, float *y, float *z, float *vx, float *vy, float *vz, uint32_t count, float dt) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= count) return;
+    // harmonic pull toward the origin with a swirl about y and linear damping
+    const float k = 4.0f, w = 0.6f, damp = 1.0f - 0.02f * dt;
+    float px = x[i], py = y[i], pz = z[i];
+    float nvx = fmaf(-k * px + w * pz, dt, vx[i]) * damp;
+    float nvy = fmaf(-k * py, dt, vy[i]) * damp;
+    float nvz = fmaf(-k * pz - w * px, dt, vz[i]) * damp;
+    vx[i] = nvx;
+    vy[i] = nvy;
+    vz[i] = nvz;
+    x[i] = fmaf(nvx, dt, px);
+    y[i] = fmaf(nvy, dt, py);
+    z[i] = fmaf(nvz, dt, pz);
+}
+}   // namespace
+
+SGB_API int32_t gpu_step_points(float *x, float *y, float *z, float *vx, float *vy, float *vz, uint32_t count, float dt) {
+    if (count == 0) return 0;
+    step_points_kernel<<<(count + 255) / 256, 256, 0, g.stream>>>(x, y, z, vx, vy, vz, count, dt);
+    return (int32_t)cudaGetLastError();
+}
+
+SGB_API int32_t gpu_kin_set_mech(const KinMech *mech, const KinMethod *method, const KinControl *control) {
+    if (!g.ready) return (int32_t)cudaErrorInitializationError;
+    if (!mech || !method || !control) return (int32_t)cudaErrorInvalidValue;
+    if (mech->species_count == 0 || mech->species_count > KIN_MAX_SPECIES || mech->reaction_count > KIN_MAX_REACTIONS ||
+        mech->nnz > KIN_MAX_NNZ || mech->lu_div_count > KIN_MAX_LU_DIV || mech->lu_sub_count > KIN_MAX_LU_SUB ||
+        method->stages < 2 || method->stages > KIN_MAX_STAGES)
+        return (int32_t)cudaErrorInvalidValue;
+    // every table index must stay inside the tables (the kernels do not re-check)
+    const uint32_t n = mech->species_count, nnz = mech->nnz;
+    if (mech->div_begin[n] != mech->lu_div_count || mech->lower_begin[n] > KIN_MAX_NNZ || mech->upper_begin[n] > KIN_MAX_NNZ)
+        return (int32_t)cudaErrorInvalidValue;
+    for (uint32_t i = 0; i < n; ++i)
+        if (mech->diag[i] >= nnz || mech->div_begin[i] > mech->div_begin[i + 1] || mech->lower_begin[i] > mech->lower_begin[i + 1] ||
+            mech->upper_begin[i] > mech->upper_begin[i + 1])
+            return (int32_t)cudaErrorInvalidValue;
+    for (uint32_t d = 0; d < mech->lu_div_count; ++d) {
+        const KinLuDiv &v = mech->lu_div[d];
+        if (v.ik >= nnz || v.kk >= nnz || v.sub_begin > v.sub_end || v.sub_end > mech->lu_sub_count) return (int32_t)cudaErrorInvalidValue;
+    }
+    for (uint32_t s = 0; s < mech->lu_sub_count; ++s)
+        if (mech->lu_sub[s].ij >= nnz || mech->lu_sub[s].kj >= nnz) return (int32_t)cudaErrorInvalidValue;
+    for (uint32_t e = 0; e < mech->lower_begin[n]; ++e)
+        if (mech->lower[e].index >= nnz || mech->lower[e].col >= n) return (int32_t)cudaErrorInvalidValue;
+    for (uint32_t e = 0; e < mech->upper_begin[n]; ++e)
+        if (mech->upper[e].index >= nnz || mech->upper[e].col >= n) return (int32_t)cudaErrorInvalidValue;
+    for (uint32_t r = 0; r < mech->reaction_count; ++r) {
+        const KinReaction &rx = mech->reactions[r];
+        if (rx.reactant_count > KIN_MAX_REACTANTS || rx.net_count > KIN_MAX_NET) return (int32_t)cudaErrorInvalidValue;
+        for (uint32_t p = 0; p < rx.reactant_count; ++p) {
+            if (rx.reactant[p] >= n) return (int32_t)cudaErrorInvalidValue;
+            for (uint32_t e = 0; e < rx.net_count; ++e)
+                if (rx.jac_index[p][e] >= nnz) return (int32_t)cudaErrorInvalidValue;
+        }
+        for (uint32_t e = 0; e < rx.net_count; ++e)
+            if (rx.net_species[e] >= n) return (int32_t)cudaErrorInvalidValue;
+    }
+    cudaError_t e = cudaMemcpyAsync(g.d_tables, mech, sizeof(KinMech), cudaMemcpyHostToDevice, g.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
+    if (e != cudaSuccess) return (int32_t)e;
+    g.mech = *mech;
+    g.method = *method;
+    g.control = *control;
+    g.generated = fnv1a(mech, sizeof(KinMech)) == air_ops_signature() && is_rodas3(method);
+    g.have_mech = true;
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_advance(const GpuKinLaunch *launch, float *kernel_ms) {
+    uint32_t p = launch ? launch->precision : 0;
+    if (p > 2) return (int32_t)cudaErrorInvalidValue;
+    return (int32_t)advance_sync(launch, g.tuning[p], kernel_ms);
+}
+
+SGB_API int32_t gpu_host_register(void *host, uint64_t size) {
+    cudaError_t e = cudaHostRegister(host, size, cudaHostRegisterDefault);
+    if (e == cudaErrorHostMemoryAlreadyRegistered) {
+        cudaGetLastError();
+        return 0;
+    }
+    return (int32_t)e;
+}
+
+SGB_API int32_t gpu_host_unregister(void *host) {
+    cudaStreamSynchronize(g.stream);
+    return (int32_t)cudaHostUnregister(host);
+}
+
+SGB_API int32_t gpu_kin_advance_async(const GpuKinLaunch *launch, void *host_block, void *device_block, uint64_t rows,
+                                      uint64_t mutable_rows) {
+    cudaError_t e = check_launch(launch);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (!host_block || !device_block || mutable_rows > rows) return (int32_t)cudaErrorInvalidValue;
+    const uint64_t pitch = (uint64_t)launch->padded * sizeof(double);
+    const uint64_t width = (uint64_t)(launch->lane_count ? launch->lane_count : launch->padded) * sizeof(double);
+    cudaEventRecord(g.async_begin, g.stream);
+    e = cudaMemcpy2DAsync(device_block, pitch, host_block, pitch, width, rows, cudaMemcpyHostToDevice, g.stream);
+    if (e != cudaSuccess) return (int32_t)e;
+    DevArgs A;
+    fill_args(launch, &A);
+    cudaEventRecord(g.kin_start, g.stream);
+    e = launch_advance(launch->precision, g.tuning[launch->precision], A);
+    cudaEventRecord(g.kin_stop, g.stream);
+    if (e != cudaSuccess) return (int32_t)e;
+    e = cudaMemcpy2DAsync(host_block, pitch, device_block, pitch, width, mutable_rows, cudaMemcpyDeviceToHost, g.stream);
+    if (e != cudaSuccess) return (int32_t)e;
+    cudaEventRecord(g.async_end, g.stream);
+    return (int32_t)cudaGetLastError();
+}
+
+SGB_API int32_t gpu_kin_wait(float *kernel_ms, float *total_ms) {
+    cudaError_t e = cudaEventSynchronize(g.async_end);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (kernel_ms) cudaEventElapsedTime(kernel_ms, g.kin_start, g.kin_stop);
+    if (total_ms) cudaEventElapsedTime(total_ms, g.async_begin, g.async_end);
+    ++g.launches;
+    e = read_error_flag();
+    if (e != cudaSuccess) return (int32_t)e;
+    return (int32_t)cudaGetLastError();
+}
+
+// Mode 1 (one warp per cell) is accepted for the reference's callers; both
+// decompositions produce the same bits, and this module runs every mode on its
+// per-lane kernels (thread per cell, optionally persistent).
+SGB_API int32_t gpu_kin_set_mode(uint32_t mode) {
+    if (mode > 1) return (int32_t)cudaErrorInvalidValue;
+    g.mode = mode;
+    return 0;
+}
+
+// ===========================================================================
+// Extra exports.
+
+SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_ms) {
+    uint32_t p = launch ? launch->precision : 0;
+    if (p > 2) return (int32_t)cudaErrorInvalidValue;
+    GpuKinTuning t = g.tuning[p];
+    t.kind = 1;
+    return (int32_t)advance_sync(launch, t, kernel_ms);
+}
+
+SGB_API int32_t gpu_kin_set_tuning(const GpuKinTuning *t) {
+    if (!t || t->kind > 1 || t->block == 0 || t->block > 128 || (t->block & 31) || t->variant > 1)
+        return (int32_t)cudaErrorInvalidValue;
+    for (int p = 0; p < 3; ++p) g.tuning[p] = *t;
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_get_tuning(uint32_t precision, GpuKinTuning *t) {
+    if (precision > 2 || !t) return (int32_t)cudaErrorInvalidValue;
+    *t = g.tuning[precision];
+    return 0;
+}
+
+// Times every (block, variant) candidate of `kind` on the caller's launch and
+// keeps the fastest for that precision. The solver-written arrays are saved
+// before and restored after each run, so the caller's data is unchanged.
+SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuKinTuning *best) {
+    cudaError_t e = check_launch(launch);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (kind > 1) return (int32_t)cudaErrorInvalidValue;
+    const uint64_t P = launch->padded, n = g.mech.species_count;
+    const uint64_t bytes_y = n * P * sizeof(double), bytes_v = P * sizeof(double);
+    double *save = nullptr;
+    e = cudaMalloc(&save, bytes_y + 5 * bytes_v);
+    if (e != cudaSuccess) return (int32_t)e;
+    double *outs[6] = {launch->y, launch->h, launch->steps, launch->rejects, launch->pulses, launch->failed};
+    uint64_t sizes[6] = {bytes_y, bytes_v, bytes_v, bytes_v, bytes_v, bytes_v};
+    auto copy_all = [&](bool to_save) {
+        uint64_t off = 0;
+        for (int i = 0; i < 6; ++i) {
+            uint8_t *s = (uint8_t *)save + off;
+            if (to_save) cudaMemcpyAsync(s, outs[i], sizes[i], cudaMemcpyDeviceToDevice, g.stream);
+            else cudaMemcpyAsync(outs[i], s, sizes[i], cudaMemcpyDeviceToDevice, g.stream);
+            off += sizes[i];
+        }
+    };
+    copy_all(true);
+    const uint32_t blocks[3] = {32, 64, 128};
+    GpuKinTuning winner = g.tuning[launch->precision];
+    winner.ms = 1e30f;
+    for (uint32_t v = 0; v < 2 && e == cudaSuccess; ++v)
+        for (uint32_t b : blocks) {
+            GpuKinTuning t = {kind, b, 1u, v, 0.0f};
+            float ms = 0.0f;
+            e = advance_sync(launch, t, &ms);
+            copy_all(false);
+            if (e != cudaSuccess) break;
+            if (ms < winner.ms) {
+                winner = t;
+                winner.ms = ms;
+            }
+        }
+    cudaStreamSynchronize(g.stream);
+    cudaFree(save);
+    if (e != cudaSuccess) return (int32_t)e;
+    g.tuning[launch->precision] = winner;
+    if (best) *best = winner;
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_last_stats(uint64_t *kernel_launches, float *last_kernel_ms) {
+    if (kernel_launches) *kernel_launches = g.launches;
+    if (last_kernel_ms) *last_kernel_ms = g.last_ms;
+    return 0;
+}
+
+// Mixed path refinement sweeps per stage solve (1 or 2).
+SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps) {
+    if (sweeps < 1 || sweeps > 2) return (int32_t)cudaErrorInvalidValue;
+    g.ir_sweeps = sweeps;
+    return 0;
+}
+
+// Measured instruction throughput (operations per second over the device):
+// kind 0 DFMA, 1 FFMA, 2 FP32<->FP64 conversion pairs, 3 DADD, 4 FP64 reciprocal, 5 FP64 sqrt.
+SGB_API int32_t gpu_probe_throughput(uint32_t kind, double *ops_per_s) {
+    if (!g.ready || !ops_per_s || kind > 5) return (int32_t)cudaErrorInvalidValue;
+    return (int32_t)run_probe(kind, g.sms, g.stream, ops_per_s);
+}
+
+// Device-to-device copy enqueued on the module stream (returns without waiting).
+SGB_API int32_t gpu_copy_on_device(void *dst_device, const void *src_device, uint64_t size) {
+    return (int32_t)cudaMemcpyAsync(dst_device, src_device, size, cudaMemcpyDeviceToDevice, g.stream);
+}
+
+// The module stream, for callers that order their own work against it.
+SGB_API void *gpu_stream(void) { return (void *)g.stream; }

@@ -1,0 +1,172 @@
+// Build-time generator: compiles a mechanism with the module's own symbolic
+// phase (mech.cpp) and writes straight-line CUDA device code for its solver
+// kernels -- the RHS, -J, the W = I/(gamma h) - J elimination and the two
+// triangular solves, plus the FP64 iterative-refinement residual of the mixed
+// path -- with every array index a compile-time constant.
+//
+//   kin_codegen <out.cuh>
+//
+// Each emitted operation is the reference table walk's operation, in the
+// same order (src/sim/kinetics/kin_solver.h:40-139; the reference's own
+// generator, src/tools/kin_codegen.cpp:32-138, does the same for the CPU), so
+// the results are bit-identical to the table walk. One exact rewrite is
+// applied: the first contribution to a zeroed Jacobian slot, fma(+-1, d, +0),
+// is emitted as an integer sign/zero fix of d (sgb_first_pos / sgb_first_neg),
+// which yields the same bits without an FP64 instruction.
+
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <string>
+#include <vector>
+
+#include "mech.h"
+
+using namespace sgb;
+
+static void emit_ops(FILE *f, Model &m, const char *name) {
+    const Symbolic &S = m.sym;
+    const uint32_t n = m.n(), R = m.R();
+    KinMech km;
+    bool fits = m.to_kinmech(&km);
+    uint64_t signature = fits ? fnv1a(&km, sizeof(km)) : 0;
+
+    // J-pattern slots (non-zeros of -J before fill-in), in compact order: the
+    // mixed path keeps a copy of them for its FP64 residual.
+    std::vector<uint32_t> jslots;
+    std::vector<uint32_t> jrow, jcol;
+    for (uint32_t i = 0; i < n; ++i)
+        for (uint32_t j = 0; j < n; ++j)
+            if (S.jac_pattern[(size_t)i * n + j]) {
+                jslots.push_back(S.slot[(size_t)i * n + j]);
+                jrow.push_back(i);
+                jcol.push_back(j);
+            }
+
+    fprintf(f, "struct %s {\n", name);
+    fprintf(f, "    static constexpr int N = %u, R = %u, NNZ = %u, NJ = %zu;\n", n, R, S.nnz, jslots.size());
+    fprintf(f, "    static constexpr unsigned long long kSignature = 0x%016llxull;\n\n", (unsigned long long)signature);
+
+    // fun: f = src + sum_r net_r k_r prod(y[reactants])
+    fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void fun(const T *__restrict__ k, const T *__restrict__ src, const T *__restrict__ y, T *__restrict__ f) {\n");
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        f[%u] = src[%u];\n", s, s);
+    for (uint32_t r = 0; r < R; ++r) {
+        const Reaction &rx = m.reactions[r];
+        fprintf(f, "        { T rate = k[%u]", r);
+        for (uint32_t q : rx.reactants) fprintf(f, " * y[%u]", q);
+        fprintf(f, ";  // %s\n", rx.equation.c_str());
+        for (auto &e : rx.net) fprintf(f, "          f[%u] = sgb_fma((T)%d.0, rate, f[%u]);\n", e.first, e.second, e.first);
+        fprintf(f, "        }\n");
+    }
+    fprintf(f, "    }\n\n");
+
+    // -J into the compact LU storage
+    fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void neg_jac(const T *__restrict__ k, const T *__restrict__ y, T *__restrict__ a) {\n");
+    std::vector<uint8_t> written(S.nnz, 0);
+    std::vector<std::string> body;
+    for (uint32_t r = 0; r < R; ++r) {
+        const Reaction &rx = m.reactions[r];
+        for (size_t p = 0; p < rx.reactants.size(); ++p) {
+            fprintf(f, "        { T d = k[%u]", r);
+            for (size_t q = 0; q < rx.reactants.size(); ++q)
+                if (q != p) fprintf(f, " * y[%u]", rx.reactants[q]);
+            fprintf(f, ";\n");
+            for (size_t e = 0; e < rx.net.size(); ++e) {
+                int c = -rx.net[e].second;
+                uint32_t idx = rx.jac_slot[p][e];
+                if (!written[idx] && (c == 1 || c == -1))
+                    fprintf(f, "          a[%u] = %s(d);\n", idx, c == 1 ? "sgb_first_pos" : "sgb_first_neg");
+                else if (!written[idx])
+                    fprintf(f, "          a[%u] = sgb_fma((T)%d.0, d, (T)0.0);\n", idx, c);
+                else
+                    fprintf(f, "          a[%u] = sgb_fma((T)%d.0, d, a[%u]);\n", idx, c, idx);
+                written[idx] = 1;
+            }
+            fprintf(f, "        }\n");
+        }
+    }
+    for (uint32_t i = 0; i < S.nnz; ++i)
+        if (!written[i]) fprintf(f, "        a[%u] = (T)0.0;\n", i);
+    fprintf(f, "    }\n\n");
+
+    // in-place no-pivot LU of I*ghinv - J; the diagonal keeps 1/U(i,i)
+    fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void factor(T ghinv, T *__restrict__ a) {\n");
+    for (uint32_t i = 0; i < n; ++i) {
+        for (uint32_t d = S.div_begin[i]; d < S.div_begin[i + 1]; ++d) {
+            const Symbolic::Div &dv = S.divs[d];
+            fprintf(f, "        { const T l = a[%u] * a[%u]; a[%u] = l;\n", dv.ik, dv.kk, dv.ik);
+            for (uint32_t s = dv.sub_begin; s < dv.sub_end; ++s)
+                fprintf(f, "          a[%u] = sgb_fma(-l, a[%u], a[%u]);\n", S.subs[s].ij, S.subs[s].kj, S.subs[s].ij);
+            fprintf(f, "        }\n");
+        }
+        fprintf(f, "        a[%u] = (T)1.0 / (a[%u] + ghinv);\n", S.diag[i], S.diag[i]);
+    }
+    fprintf(f, "    }\n\n");
+
+    // forward (unit L, ascending column) and backward (U, descending column)
+    fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void solve(const T *__restrict__ a, T *__restrict__ x) {\n");
+    for (uint32_t i = 0; i < n; ++i)
+        for (uint32_t e = S.lower_begin[i]; e < S.lower_begin[i + 1]; ++e)
+            fprintf(f, "        x[%u] = sgb_fma(-a[%u], x[%u], x[%u]);\n", i, S.lower[e].index, S.lower[e].col, i);
+    for (uint32_t ii = n; ii-- > 0;) {
+        for (uint32_t e = S.upper_begin[ii]; e < S.upper_begin[ii + 1]; ++e)
+            fprintf(f, "        x[%u] = sgb_fma(-a[%u], x[%u], x[%u]);\n", ii, S.upper[e].index, S.upper[e].col, ii);
+        fprintf(f, "        x[%u] = x[%u] * a[%u];\n", ii, ii, S.diag[ii]);
+    }
+    fprintf(f, "    }\n\n");
+
+    // mixed path: keep -J's pattern entries (FP32) before the factorisation
+    fprintf(f, "    static __device__ __forceinline__ void save_jac(const float *__restrict__ a, float *__restrict__ js) {\n");
+    for (size_t q = 0; q < jslots.size(); ++q) fprintf(f, "        js[%zu] = a[%u];\n", q, jslots[q]);
+    fprintf(f, "    }\n\n");
+    // r = b - W x = b - ghinv x - (-J) x, in FP64 (the -J entries are exact FP32 values)
+    fprintf(f, "    static __device__ __forceinline__ void residual(const float *__restrict__ js, double ghinv, const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r) {\n");
+    for (uint32_t i = 0; i < n; ++i) {
+        fprintf(f, "        { double acc = sgb_fma(-ghinv, x[%u], b[%u]);\n", i, i);
+        for (size_t q = 0; q < jslots.size(); ++q)
+            if (jrow[q] == i) fprintf(f, "          acc = sgb_fma(-(double)js[%zu], x[%u], acc);\n", q, jcol[q]);
+        fprintf(f, "          r[%u] = acc; }\n", i);
+    }
+    fprintf(f, "    }\n");
+    fprintf(f, "};\n\n");
+}
+
+int main(int argc, char **argv) {
+    if (argc < 2) {
+        fprintf(stderr, "usage: kin_codegen out.cuh\n");
+        return 1;
+    }
+    Model air;
+    define_air(&air);
+    if (!air.finalize()) {
+        fprintf(stderr, "kin_codegen: mechanism error: %s\n", air.error.c_str());
+        return 1;
+    }
+    std::string tmp = std::string(argv[1]) + ".tmp";
+    FILE *f = fopen(tmp.c_str(), "wb");
+    if (!f) {
+        fprintf(stderr, "kin_codegen: cannot write %s\n", tmp.c_str());
+        return 1;
+    }
+    fprintf(f, "// GENERATED by simstack_gb300/csrc/kin_codegen.cpp -- do not edit.\n");
+    fprintf(f, "// Straight-line solver kernels for the shipped humid-air mechanism.\n");
+    fprintf(f, "#pragma once\n\n");
+    emit_ops(f, air, "AirOps");
+    fclose(f);
+    // replace only when changed, so unchanged builds stay unchanged
+    FILE *old = fopen(argv[1], "rb"), *nw = fopen(tmp.c_str(), "rb");
+    bool same = old != nullptr;
+    if (old) {
+        for (;;) {
+            int a = fgetc(old), b = fgetc(nw);
+            if (a != b) { same = false; break; }
+            if (a == EOF) break;
+        }
+        fclose(old);
+    }
+    fclose(nw);
+    if (same) remove(tmp.c_str());
+    else rename(tmp.c_str(), argv[1]);
+    return 0;
+}

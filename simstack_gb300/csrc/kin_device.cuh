@@ -1,0 +1,482 @@
+// Device side of the batched Rosenbrock integrator.
+//
+// One lane = one cell (an independent reactor). A lane's integration over
+// [0, duration] is written as a small state machine -- segment start, one
+// step attempt, segment end (discharge pulse), done -- so that a kernel can
+// run each lane's attempts back to back and refill a lane with a new cell the
+// moment its cell finishes (the persistent work-queue kernel), while every
+// lane still performs exactly the operation sequence of the reference's
+// scalar lane:
+//   kin_integrate  src/sim/kinetics/kin_solver.h:189-313 (one attempt = one
+//                  pass of its while loop, lines 211-312)
+//   kin_advance    kin_solver.h:322-347 (segments between pulses)
+//   dbd_advance_group  src/sim/dbd_lanes.h:28-78 (load / store, counters
+//                  accumulate, f32 lanes store base + increment)
+// Precisions (GpuKinLaunch.precision):
+//   0  f64 lanes: every operation the reference's f64 lane performs, built with
+//      -fmad=false so FMAs appear only where the reference has lane_fmadd; the
+//      result is bit-identical to the reference's CPU path
+//   1  f32 lanes, Delta formulation (the reference's f32 / f32x8 lanes)
+//   2  mixed: RHS, -J and the LU of W in FP32; each stage solve refined with
+//      FP64-residual iterative refinement; state, stage combination, error
+//      estimate and step-size control in FP64 (the same controller code as 0)
+
+#pragma once
+#include <stdint.h>
+
+#include "../../include/simstack_gpu.h"
+#include "ptx.cuh"
+
+namespace sgb {
+
+// ---------------------------------------------------------------------------
+// Lane arithmetic with the reference's semantics (src/base/base_lane.h:253-341).
+
+__device__ __forceinline__ double sgb_fma(double a, double b, double c) { return fma(a, b, c); }
+__device__ __forceinline__ float sgb_fma(float a, float b, float c) { return fmaf(a, b, c); }
+template <class T> __device__ __forceinline__ T vmin(T a, T b) { return a < b ? a : b; }
+template <class T> __device__ __forceinline__ T vmax(T a, T b) { return a > b ? a : b; }
+template <class T> __device__ __forceinline__ T vabs(T a) { return a < (T)0 ? -a : a; }
+__device__ __forceinline__ double vsqrt(double a) { return sqrt(a); }
+__device__ __forceinline__ float vsqrt(float a) { return sqrtf(a); }
+template <class T> __device__ __forceinline__ bool is_finite_lane(T a) {
+    T d = a - a;
+    return d == d;
+}
+
+// fma(+1, d, +0) and fma(-1, d, +0), exactly, with integer operations: the
+// product is exact, and the only case the +0 addend changes is a zero product,
+// which becomes +0. (Used for the first term of each Jacobian slot.)
+__device__ __forceinline__ double sgb_first_pos(double d) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return __longlong_as_double((long long)((b << 1) == 0 ? 0ull : b));
+}
+__device__ __forceinline__ double sgb_first_neg(double d) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(d);
+    return __longlong_as_double((long long)((b << 1) == 0 ? 0ull : (b ^ 0x8000000000000000ull)));
+}
+__device__ __forceinline__ float sgb_first_pos(float d) {
+    unsigned b = __float_as_uint(d);
+    return __uint_as_float((b << 1) == 0 ? 0u : b);
+}
+__device__ __forceinline__ float sgb_first_neg(float d) {
+    unsigned b = __float_as_uint(d);
+    return __uint_as_float((b << 1) == 0 ? 0u : (b ^ 0x80000000u));
+}
+
+// x^(1/3) on [1e-4, 1e4]: x^(1/4) x^(1/16) x^(1/64) from six square roots,
+// then two Newton steps; no libm (base_lane.h:123-135).
+template <class T> __device__ __forceinline__ T cbrt_clamped(T x) {
+    x = vmin(vmax(x, (T)1e-4), (T)1e4);
+    T r4 = vsqrt(vsqrt(x));
+    T r16 = vsqrt(vsqrt(r4));
+    T r64 = vsqrt(vsqrt(r16));
+    T g = r4 * r16 * r64;
+    const T two = (T)2.0, third = (T)(1.0 / 3.0);
+    g = (two * g + x / (g * g)) * third;
+    g = (two * g + x / (g * g)) * third;
+    return g;
+}
+
+// (1/err)^(1/order) * 0.9 clamped to [0.2, 6] (kin_solver.h:169-180).
+template <class T> __device__ __forceinline__ T step_factor(T err, uint32_t order) {
+    T e = vmin(vmax(err, (T)1e-4), (T)1e4);
+    T root;
+    if (order == 2) root = vsqrt(e);
+    else if (order == 4) root = vsqrt(vsqrt(e));
+    else root = cbrt_clamped(e);
+    T fac = (T)0.9 / root;
+    return vmin(vmax(fac, (T)0.2), (T)6.0);
+}
+
+// ---------------------------------------------------------------------------
+// Launch arguments (kernel parameter space: uniform, constant-bank reads).
+
+struct DevArgs {
+    double *y, *h, *steps, *rejects, *pulses, *failed;
+    const double *k, *src, *pulse, *period, *pulse_first, *pulse_count;
+    uint32_t padded, lanes;
+    double duration;
+    KinControl ctl;
+    double ma[6], mc[6], mm[4], me[4], gamma0;
+    int32_t new_f[4];
+    uint32_t stages, order;
+    uint32_t ir_sweeps;        // mixed path: refinement sweeps per stage solve (>= 1)
+    uint32_t *cursor;          // queue kernel: next unclaimed lane
+    uint32_t *error_flag;      // nonzero: a bounded wait ran out (tables not staged)
+    const void *tables;        // table-driven ops: KinMech image in global memory
+    uint32_t table_bytes;      // bytes to stage (multiple of 16)
+};
+
+// Method coefficients known at compile time (Rodas3: kin_solver.h:382-391) or
+// read from the launch arguments (any method).
+struct Rodas3Coef {
+    static constexpr int kStages = 4;
+    __device__ static constexpr int stages(const DevArgs &) { return 4; }
+    __device__ static constexpr uint32_t order(const DevArgs &) { return 3; }
+    __device__ static constexpr double a(const DevArgs &, int i) { return i == 1 ? 2.0 : i == 3 ? 2.0 : i == 5 ? 1.0 : 0.0; }
+    __device__ static constexpr double c(const DevArgs &, int i) {
+        return i == 0 ? 4.0 : i == 1 ? 1.0 : i == 2 ? -1.0 : i == 3 ? 1.0 : i == 4 ? -1.0 : -8.0 / 3.0;
+    }
+    __device__ static constexpr double m(const DevArgs &, int i) { return i == 0 ? 2.0 : i == 1 ? 0.0 : 1.0; }
+    __device__ static constexpr double e(const DevArgs &, int i) { return i == 3 ? 1.0 : 0.0; }
+    __device__ static constexpr double gamma0(const DevArgs &) { return 0.5; }
+    __device__ static constexpr bool new_f(const DevArgs &, int) { return true; }
+};
+
+// Any method of up to KIN_MAX_STAGES stages; the stage count is a runtime bound.
+struct RuntimeCoef {
+    static constexpr int kStages = KIN_MAX_STAGES;
+    __device__ static int stages(const DevArgs &A) { return (int)A.stages; }
+    __device__ static uint32_t order(const DevArgs &A) { return A.order; }
+    __device__ static double a(const DevArgs &A, int i) { return A.ma[i]; }
+    __device__ static double c(const DevArgs &A, int i) { return A.mc[i]; }
+    __device__ static double m(const DevArgs &A, int i) { return A.mm[i]; }
+    __device__ static double e(const DevArgs &A, int i) { return A.me[i]; }
+    __device__ static double gamma0(const DevArgs &A) { return A.gamma0; }
+    __device__ static bool new_f(const DevArgs &A, int i) { return A.new_f[i] != 0; }
+};
+
+template <bool B, class X, class Y> struct Pick { typedef X type; };
+template <class X, class Y> struct Pick<false, X, Y> { typedef Y type; };
+
+enum : int { kPhaseSegStart = 0, kPhaseStepping = 1, kPhaseSegFinish = 2, kPhaseDone = 3 };
+
+// ---------------------------------------------------------------------------
+// One lane. Ops provides the mechanism kernels (generated straight-line code
+// or the table walk); M the method coefficients; PREC the precision.
+
+template <class Ops, class M, int PREC>
+struct Lane {
+    typedef typename Pick<PREC == 1, float, double>::type T;    // time, step size, state, stage vectors
+    typedef typename Pick<PREC == 0, double, float>::type Cf;   // RHS / Jacobian / LU arithmetic
+    static constexpr bool kDelta = PREC == 1;
+    static constexpr bool kMixed = PREC == 2;
+    static constexpr int N = Ops::N, R = Ops::R, NNZ = Ops::NNZ, S = M::kStages;
+
+    Ops ops;
+    // cell data
+    T y[N];
+    T base[kDelta ? N : 1];
+    Cf k[R], src[N];
+    T t, h, seg_end, applied, duration, period, first, count;
+    T steps, rejects, pulses, failed;
+    uint32_t iterations, transitions;
+    int phase;
+    bool pending, reject_last, reject_more;
+    // per-attempt scratch
+    Cf lu[NNZ];
+    Cf fcn[N];
+    Cf ceval[kMixed || kDelta ? N : 1];      // f32 evaluation point (mixed) / base + increment (delta)
+    T ytmp[N];
+    T K[S][N];
+    float js[kMixed ? Ops::NJ : 1];            // mixed: -J pattern entries before the factorisation
+    double rb[kMixed ? N : 1];                 // mixed: stage right-hand side b
+    double rr[kMixed ? N : 1];                 // mixed: residual
+    float x32[kMixed ? N : 1];
+
+    __device__ __forceinline__ uint32_t n() const { return ops.n(); }
+
+    // dbd_lanes.h:28-58: storage is f64; f32 lanes round on load.
+    __device__ __forceinline__ void load(const DevArgs &A, uint32_t i) {
+        const uint32_t p = A.padded, nn = n(), rr_ = ops.r();
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            double v = A.y[(size_t)s * p + i];
+            if (kDelta) {
+                base[s] = (T)v;
+                y[s] = (T)0.0;
+            } else {
+                y[s] = (T)v;
+            }
+            src[s] = (Cf)A.src[(size_t)s * p + i];
+        }
+        for (int r = 0; r < R; ++r) {
+            if (r >= (int)rr_) break;
+            k[r] = (Cf)A.k[(size_t)r * p + i];
+        }
+        h = (T)A.h[i];
+        period = (T)A.period[i];
+        first = (T)A.pulse_first[i];
+        count = (T)A.pulse_count[i];
+        duration = (T)A.duration;
+        steps = rejects = pulses = (T)0.0;
+        failed = (T)A.failed[i];
+        t = (T)0.0;
+        applied = (T)0.0;
+        transitions = 0;
+        phase = kPhaseSegStart;
+    }
+
+    // dbd_lanes.h:60-77: f32 lanes add their increment to the f64 storage.
+    __device__ __forceinline__ void store(const DevArgs &A, uint32_t i) {
+        const uint32_t p = A.padded, nn = n();
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            double *dst = A.y + (size_t)s * p + i;
+            if (kDelta) {
+                double v = *dst + (double)y[s];
+                if (A.ctl.clamp_negative) v = v > 0.0 ? v : 0.0;
+                *dst = v;
+            } else {
+                *dst = (double)y[s];
+            }
+        }
+        A.h[i] = (double)h;
+        A.failed[i] = (double)failed;
+        A.steps[i] += (double)steps;
+        A.rejects[i] += (double)rejects;
+        A.pulses[i] += (double)pulses;
+    }
+
+    // kin_advance segment start + kin_integrate prologue (kin_solver.h:204-208, 330-334).
+    __device__ __forceinline__ void seg_start(const DevArgs &A) {
+        const T zero = (T)0.0;
+        pending = applied < count;
+        T next_pulse = sgb_fma(applied, period, first);
+        seg_end = pending ? vmin(next_pulse, duration) : duration;
+        bool active = t < seg_end && !(failed > zero);
+        reject_last = false;
+        reject_more = false;
+        h = h > zero ? h : (T)A.ctl.h_start;
+        iterations = 0;
+        phase = active ? kPhaseStepping : kPhaseSegFinish;
+    }
+
+    // kin_advance after one segment (kin_solver.h:336-345).
+    __device__ __forceinline__ void seg_finish(const DevArgs &A, uint32_t cell) {
+        const T zero = (T)0.0, one = (T)1.0;
+        bool alive = !(failed > zero);
+        bool hit = pending && alive && t >= seg_end;
+        if (hit) {
+            const uint32_t p = A.padded, nn = n();
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                y[s] = y[s] + (T)A.pulse[(size_t)s * p + cell];
+            }
+            applied = applied + one;
+            pulses = pulses + one;
+            h = (T)A.ctl.h_start;
+        }
+        bool done = (t >= duration && applied >= count) || !alive;
+        phase = done ? kPhaseDone : kPhaseSegStart;
+    }
+
+    // Runs the cheap transitions until the lane needs a step attempt (true)
+    // or has finished its cell (false). The transition guard only ends cells
+    // whose pulse schedule cannot terminate (non-finite counts).
+    __device__ __forceinline__ bool settle(const DevArgs &A, uint32_t cell) {
+        for (;;) {
+            if (++transitions > (1u << 30)) {
+                failed = (T)1.0;
+                phase = kPhaseDone;
+            }
+            switch (phase) {
+                case kPhaseSegStart: seg_start(A); break;
+                case kPhaseSegFinish: seg_finish(A, cell); break;
+                case kPhaseStepping:
+                    if (++iterations > A.ctl.max_steps) {   // kin_solver.h:212-215
+                        failed = (T)1.0;
+                        phase = kPhaseSegFinish;
+                        break;
+                    }
+                    return true;
+                default: return false;
+            }
+        }
+    }
+
+    __device__ __forceinline__ void eval_point(const T *yy, const Cf *&at) {
+        const uint32_t nn = n();
+        if constexpr (kDelta) {
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                ceval[s] = base[s] + yy[s];
+            }
+            at = ceval;
+        } else if constexpr (kMixed) {
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                ceval[s] = (Cf)yy[s];
+            }
+            at = ceval;
+        } else {
+            at = yy;
+        }
+    }
+
+    // Mixed path: x = W^-1 b with the FP32 LU, then `sweeps` refinement
+    // sweeps x += W^-1 (b - W x), residual in FP64. b in rb, result in x.
+    __device__ __forceinline__ void solve_refined(const DevArgs &A, double ghinv, double *x) {
+        const uint32_t nn = n();
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            x32[s] = (float)rb[s];
+        }
+        ops.solve(lu, x32);
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            x[s] = (double)x32[s];
+        }
+        for (uint32_t sw = 0; sw < A.ir_sweeps; ++sw) {
+            ops.residual(js, ghinv, rb, x, rr);
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                x32[s] = (float)rr[s];
+            }
+            ops.solve(lu, x32);
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                x[s] = x[s] + (double)x32[s];
+            }
+        }
+    }
+
+    // One pass of kin_integrate's step loop (kin_solver.h:216-311) for an active lane.
+    __device__ __forceinline__ void attempt(const DevArgs &A) {
+        const T zero = (T)0.0, one = (T)1.0;
+        const uint32_t nn = n();
+        const T h_min = (T)A.ctl.h_min, rtol = (T)A.ctl.rtol, atol = (T)A.ctl.atol;
+        const T inv_n = (T)(1.0 / (double)nn);
+
+        T remaining = seg_end - t;
+        T h_cap = remaining;
+        if (A.ctl.h_max > 0.0) h_cap = vmin(h_cap, (T)A.ctl.h_max);
+        T h_wanted = vmax(h, h_min);
+        bool last = h_wanted >= remaining;
+        T hs = last ? remaining : vmin(h_wanted, h_cap);
+
+        const Cf *at;
+        eval_point(y, at);
+        ops.fun(k, src, at, fcn);
+        ops.neg_jac(k, at, lu);
+        if constexpr (kMixed) ops.save_jac(lu, js);
+        T ghinv = one / (hs * (T)M::gamma0(A));
+        ops.factor((Cf)ghinv, lu);
+        T hinv = one / hs;
+
+#pragma unroll
+        for (int st = 0; st < S; ++st) {
+            if (st >= M::stages(A)) break;
+            const int packed = st * (st - 1) / 2;
+            if (st > 0 && M::new_f(A, st)) {
+                for (int s = 0; s < N; ++s) {
+                    if (s >= (int)nn) break;
+                    ytmp[s] = y[s];
+                }
+#pragma unroll
+                for (int j = 0; j < st; ++j) {
+                    double a = M::a(A, packed + j);
+                    if (a == 0.0) continue;
+                    T av = (T)a;
+                    for (int s = 0; s < N; ++s) {
+                        if (s >= (int)nn) break;
+                        ytmp[s] = sgb_fma(av, K[j][s], ytmp[s]);
+                    }
+                }
+                eval_point(ytmp, at);
+                ops.fun(k, src, at, fcn);
+            }
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                K[st][s] = (T)fcn[s];
+            }
+#pragma unroll
+            for (int j = 0; j < st; ++j) {
+                double c = M::c(A, packed + j);
+                if (c == 0.0) continue;
+                T hc = (T)c * hinv;
+                for (int s = 0; s < N; ++s) {
+                    if (s >= (int)nn) break;
+                    K[st][s] = sgb_fma(hc, K[j][s], K[st][s]);
+                }
+            }
+            if constexpr (kMixed) {
+                for (int s = 0; s < N; ++s) {
+                    if (s >= (int)nn) break;
+                    rb[s] = K[st][s];
+                }
+                solve_refined(A, ghinv, K[st]);
+            } else {
+                ops.solve(lu, K[st]);
+            }
+        }
+
+        // y_new into ytmp and the weighted RMS error (kin_solver.h:263-280)
+        T err = zero;
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            T ynew = y[s], yerr = zero;
+            bool first_e = true;
+#pragma unroll
+            for (int st = 0; st < S; ++st) {
+                if (st >= M::stages(A)) break;
+                const double mc = M::m(A, st), ec = M::e(A, st);
+                if (mc != 0.0) ynew = sgb_fma((T)mc, K[st][s], ynew);
+                if (ec != 0.0) {
+                    yerr = (first_e && ec == 1.0) ? sgb_first_pos(K[st][s]) : sgb_fma((T)ec, K[st][s], yerr);
+                    first_e = false;
+                }
+            }
+            T scale;
+            if (kDelta) scale = sgb_fma(rtol, vmax(vabs(base[s] + y[s]), vabs(base[s] + ynew)), atol);
+            else scale = sgb_fma(rtol, vmax(vabs(y[s]), vabs(ynew)), atol);
+            T q = yerr / scale;
+            err = sgb_fma(q, q, err);
+            ytmp[s] = ynew;
+        }
+        err = vsqrt(err * inv_n);
+        if (!is_finite_lane(err)) err = (T)1e10;
+
+        T fac = step_factor(err, M::order(A));
+        bool ok = err <= one || hs <= h_min;
+        if (A.ctl.fixed_step) {
+            ok = true;
+            fac = one;
+        }
+        if (ok) {
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                T ynew = ytmp[s];
+                if (A.ctl.clamp_negative) ynew = kDelta ? vmax(ynew, -base[s]) : vmax(ynew, zero);
+                y[s] = ynew;
+            }
+            t = last ? seg_end : t + hs;
+        }
+        T h_acc = hs * fac;
+        h_acc = reject_last ? vmin(h_acc, hs) : h_acc;
+        h_acc = (last && fac >= one) ? vmax(h_acc, h_wanted) : h_acc;
+        T h_rej = reject_more ? hs * (T)0.1 : vmin(hs * fac, hs);
+        if (A.ctl.fixed_step) {
+            h_acc = h_wanted;
+            h_rej = h_wanted;
+        }
+        h = ok ? h_acc : h_rej;
+        reject_more = !ok && reject_last;
+        reject_last = !ok;
+        steps = steps + (ok ? one : zero);
+        rejects = rejects + (ok ? zero : one);
+        if (!(t < seg_end && !(failed > zero))) phase = kPhaseSegFinish;
+    }
+};
+
+// ---------------------------------------------------------------------------
+// Generated straight-line ops (kin_codegen.cpp) as an Ops object.
+
+template <class G>
+struct GenOps {
+    static constexpr int N = G::N, R = G::R, NNZ = G::NNZ, NJ = G::NJ;
+    __device__ __forceinline__ uint32_t n() const { return (uint32_t)N; }
+    __device__ __forceinline__ uint32_t r() const { return (uint32_t)R; }
+    __device__ __forceinline__ bool init(const DevArgs &, unsigned char *) { return true; }
+    template <class T> __device__ __forceinline__ void fun(const T *k, const T *src, const T *y, T *f) const { G::fun(k, src, y, f); }
+    template <class T> __device__ __forceinline__ void neg_jac(const T *k, const T *y, T *a) const { G::neg_jac(k, y, a); }
+    template <class T> __device__ __forceinline__ void factor(T ghinv, T *a) const { G::factor(ghinv, a); }
+    template <class T> __device__ __forceinline__ void solve(const T *a, T *x) const { G::solve(a, x); }
+    __device__ __forceinline__ void save_jac(const float *a, float *js) const { G::save_jac(a, js); }
+    __device__ __forceinline__ void residual(const float *js, double ghinv, const double *b, const double *x, double *r) const {
+        G::residual(js, ghinv, b, x, r);
+    }
+};
+
+}   // namespace sgb

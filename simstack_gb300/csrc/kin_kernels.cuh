@@ -1,0 +1,106 @@
+// Kernels of the batched integrator, instantiated per (ops, method, precision)
+// in separate translation units so the module builds in parallel.
+//
+//   static  one cell per thread, grid = ceil(lanes / block): the reference's
+//           launch shape (src/gpu/kernels.cu:263-274), each thread running its
+//           cell to completion
+//   queue   persistent: grid = SMs x resident CTAs; each thread claims a cell
+//           from a device work queue (atomic cursor), runs it, and claims the
+//           next the moment it finishes, so lanes whose cells need few steps do
+//           not sit idle beside stiff ones (warp lanes stay busy, CTAs never
+//           wait for a tail of long cells)
+// Register-budget variants: 0 = __launch_bounds__(128, 1) (up to 255 regs),
+// 1 = __launch_bounds__(128, 4) (128 regs).
+
+#pragma once
+#include <cuda_runtime.h>
+
+#include "kin_device.cuh"
+
+namespace sgb {
+
+template <int V> struct Budget;
+template <> struct Budget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
+template <> struct Budget<1> { static constexpr int kThreads = 128, kMinBlocks = 4; };
+
+template <class Ops, class M, int PREC, int V>
+__global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_static_kernel(const __grid_constant__ DevArgs A) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    Lane<Ops, M, PREC> L;
+    if (!L.ops.init(A, smem)) {
+        if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
+        return;
+    }
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= A.lanes) return;
+    L.load(A, i);
+    while (L.settle(A, i)) L.attempt(A);
+    L.store(A, i);
+}
+
+template <class Ops, class M, int PREC, int V>
+__global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_queue_kernel(const __grid_constant__ DevArgs A) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    Lane<Ops, M, PREC> L;
+    if (!L.ops.init(A, smem)) {
+        if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
+        return;
+    }
+    bool have = false;
+    uint32_t cell = 0;
+    for (;;) {
+        bool need = false;
+        for (;;) {
+            if (!have) {
+                cell = atomicAdd(A.cursor, 1u);
+                if (cell >= A.lanes) break;
+                L.load(A, cell);
+                have = true;
+            }
+            if (L.settle(A, cell)) {
+                need = true;
+                break;
+            }
+            L.store(A, cell);
+            have = false;
+        }
+        if (!need) break;
+        L.attempt(A);
+    }
+}
+
+// Launch shape chosen by the host (module tuning or the autotuner).
+struct Shape {
+    uint32_t kind;      // 0 static, 1 queue
+    uint32_t block;     // threads per CTA, multiple of 32, <= 128
+    uint32_t grid;      // CTAs
+    uint32_t variant;   // register budget
+    size_t smem;        // dynamic shared memory (table ops: staged tables)
+};
+
+// kVariants: how many register-budget variants are instantiated (1: variant 0 only).
+template <class Ops, class M, int PREC, int kVariants>
+void (*kernel_for(uint32_t kind, uint32_t variant))(DevArgs) {
+    if (kVariants > 1 && variant == 1)
+        return kind == 0 ? kin_static_kernel<Ops, M, PREC, (kVariants > 1 ? 1 : 0)> : kin_queue_kernel<Ops, M, PREC, (kVariants > 1 ? 1 : 0)>;
+    return kind == 0 ? kin_static_kernel<Ops, M, PREC, 0> : kin_queue_kernel<Ops, M, PREC, 0>;
+}
+
+template <class Ops, class M, int PREC, int kVariants = 2>
+cudaError_t launch_one(const Shape &s, const DevArgs &A, cudaStream_t stream) {
+    void (*fn)(DevArgs) = kernel_for<Ops, M, PREC, kVariants>(s.kind, s.variant);
+    if (s.smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+        if (e != cudaSuccess) return e;
+    }
+    fn<<<s.grid, s.block, s.smem, stream>>>(A);
+    return cudaGetLastError();
+}
+
+template <class Ops, class M, int PREC, int kVariants = 2>
+cudaError_t occupancy_one(uint32_t kind, uint32_t variant, uint32_t block, size_t smem, int *blocks_per_sm) {
+    void (*fn)(DevArgs) = kernel_for<Ops, M, PREC, kVariants>(kind, variant);
+    return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, (int)block, smem);
+}
+
+}   // namespace sgb

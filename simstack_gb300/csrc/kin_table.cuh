@@ -1,0 +1,126 @@
+// Table-driven mechanism ops: any mechanism that fits the reference's KinMech
+// capacities (32 species, 96 reactions, 512 non-zeros), walking its index
+// tables in the reference's order (src/sim/kinetics/kin_solver.h:40-139).
+// The KinMech image is staged once per CTA from global into shared memory with
+// a TMA bulk copy (cp.async.bulk + mbarrier); every thread then reads the same
+// table entries (broadcast, no bank conflicts).
+
+#pragma once
+#include "kin_device.cuh"
+
+namespace sgb {
+
+constexpr uint32_t kTableBytes = (uint32_t)((sizeof(KinMech) + 15) / 16 * 16);
+
+struct TableOps {
+    static constexpr int N = KIN_MAX_SPECIES, R = KIN_MAX_REACTIONS, NNZ = KIN_MAX_NNZ, NJ = KIN_MAX_NNZ;
+    const KinMech *m;
+
+    __device__ __forceinline__ uint32_t n() const { return m->species_count; }
+    __device__ __forceinline__ uint32_t r() const { return m->reaction_count; }
+
+    // Stages the tables; every thread of the CTA calls it. False if the bounded
+    // wait for the copy ran out (the caller then records the error and returns).
+    __device__ bool init(const DevArgs &A, unsigned char *smem) {
+        __shared__ __align__(8) uint64_t bar;
+        m = (const KinMech *)smem;
+        if (threadIdx.x == 0) {
+            mbar_init(&bar, 1);
+            fence_mbar_init();
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            mbar_arrive_expect_tx(&bar, A.table_bytes);
+            tma_bulk_g2s(smem, A.tables, A.table_bytes, &bar);
+        }
+        bool ok = mbar_wait(&bar, 0);
+        __syncthreads();
+        return ok;
+    }
+
+    template <class T> __device__ __forceinline__ void fun(const T *k, const T *src, const T *y, T *f) const {
+        const uint32_t ns = m->species_count, nr = m->reaction_count;
+        for (uint32_t s = 0; s < ns; ++s) f[s] = src[s];
+        for (uint32_t r = 0; r < nr; ++r) {
+            const KinReaction &rx = m->reactions[r];
+            T rate = k[r];
+            for (uint32_t p = 0; p < rx.reactant_count; ++p) rate = rate * y[rx.reactant[p]];
+            for (uint32_t e = 0; e < rx.net_count; ++e) {
+                uint32_t s = rx.net_species[e];
+                f[s] = sgb_fma((T)(double)rx.net_coef[e], rate, f[s]);
+            }
+        }
+    }
+
+    template <class T> __device__ __forceinline__ void neg_jac(const T *k, const T *y, T *a) const {
+        const uint32_t nz = m->nnz, nr = m->reaction_count;
+        for (uint32_t i = 0; i < nz; ++i) a[i] = (T)0.0;
+        for (uint32_t r = 0; r < nr; ++r) {
+            const KinReaction &rx = m->reactions[r];
+            for (uint32_t p = 0; p < rx.reactant_count; ++p) {
+                T d = k[r];
+                for (uint32_t q = 0; q < rx.reactant_count; ++q)
+                    if (q != p) d = d * y[rx.reactant[q]];
+                for (uint32_t e = 0; e < rx.net_count; ++e) {
+                    uint32_t idx = rx.jac_index[p][e];
+                    a[idx] = sgb_fma((T)(-(double)rx.net_coef[e]), d, a[idx]);
+                }
+            }
+        }
+    }
+
+    template <class T> __device__ __forceinline__ void factor(T ghinv, T *a) const {
+        const uint32_t ns = m->species_count;
+        for (uint32_t i = 0; i < ns; ++i) {
+            for (uint32_t d = m->div_begin[i]; d < m->div_begin[i + 1]; ++d) {
+                const KinLuDiv dv = m->lu_div[d];
+                T l = a[dv.ik] * a[dv.kk];
+                a[dv.ik] = l;
+                for (uint32_t s = dv.sub_begin; s < dv.sub_end; ++s) {
+                    const KinLuSub sb = m->lu_sub[s];
+                    a[sb.ij] = sgb_fma(-l, a[sb.kj], a[sb.ij]);
+                }
+            }
+            uint32_t ii = m->diag[i];
+            a[ii] = (T)1.0 / (a[ii] + ghinv);
+        }
+    }
+
+    template <class T> __device__ __forceinline__ void solve(const T *a, T *x) const {
+        const uint32_t ns = m->species_count;
+        for (uint32_t i = 0; i < ns; ++i)
+            for (uint32_t e = m->lower_begin[i]; e < m->lower_begin[i + 1]; ++e) {
+                const KinRowEntry le = m->lower[e];
+                x[i] = sgb_fma(-a[le.index], x[le.col], x[i]);
+            }
+        for (uint32_t ii = ns; ii-- > 0;) {
+            for (uint32_t e = m->upper_begin[ii]; e < m->upper_begin[ii + 1]; ++e) {
+                const KinRowEntry ue = m->upper[e];
+                x[ii] = sgb_fma(-a[ue.index], x[ue.col], x[ii]);
+            }
+            x[ii] = x[ii] * a[m->diag[ii]];
+        }
+    }
+
+    // Mixed path: keep all of -J (fill-in slots are zero) before the factorisation.
+    __device__ __forceinline__ void save_jac(const float *a, float *js) const {
+        const uint32_t nz = m->nnz;
+        for (uint32_t i = 0; i < nz; ++i) js[i] = a[i];
+    }
+
+    // r = b - ghinv x - (-J) x in FP64.
+    __device__ __forceinline__ void residual(const float *js, double ghinv, const double *b, const double *x, double *r) const {
+        const uint32_t ns = m->species_count;
+        for (uint32_t i = 0; i < ns; ++i) {
+            double acc = sgb_fma(-ghinv, x[i], b[i]);
+            acc = sgb_fma(-(double)js[m->diag[i]], x[i], acc);
+            for (uint32_t e = m->lower_begin[i]; e < m->lower_begin[i + 1]; ++e)
+                acc = sgb_fma(-(double)js[m->lower[e].index], x[m->lower[e].col], acc);
+            for (uint32_t e = m->upper_begin[i]; e < m->upper_begin[i + 1]; ++e)
+                acc = sgb_fma(-(double)js[m->upper[e].index], x[m->upper[e].col], acc);
+            r[i] = acc;
+        }
+    }
+};
+
+}   // namespace sgb

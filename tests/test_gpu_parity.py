@@ -1,0 +1,225 @@
+"""Parity of the GPU module with the CPU oracle, through the C ABI.
+
+Plain FP64 lanes (precision 0) and f32 Delta lanes (precision 1) must be
+bit-identical to the oracle (which is pinned bit for bit to the reference's own
+CPU solver); the mixed path (precision 2) is checked against the FP64 oracle
+with a stated tolerance.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import simstack_gb300 as sg
+
+pytestmark = pytest.mark.gpu
+
+STATE = ("y", "h", "steps", "rejects", "pulses", "failed")
+
+
+def oracle_run(O, z, duration, precision=0, method="rodas3", ctl=None, mech=None):
+    m = mech if mech is not None else O.Mechanism.air()
+    m.advance(method, ctl if ctl is not None else O.control(), z.as_dict(), z.padded, 0, z.padded, duration, precision, 0)
+
+
+def assert_bits(a, b, names=STATE):
+    for name in names:
+        x, y = a[name], b[name]
+        assert x.tobytes() == y.tobytes(), f"{name}: {np.count_nonzero(x != y)} entries differ"
+
+
+@pytest.mark.parametrize("kind", [0, 1], ids=["static", "queue"])
+def test_f64_bit_identical_config1(module, oracle_lib, kind):
+    """4,096-cell config-1 inputs (1 s, rtol 1e-4): every output bit equal to the oracle."""
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    module.set_tuning(kind=kind, block=128, variant=0)
+    z = sg.air_cells(4096, seed=1)
+    ref = z.copy()
+    module.integrate(z, 1.0, precision=0)
+    oracle_run(oracle_lib, ref, 1.0)
+    assert_bits(z, ref)
+    assert ref["steps"].min() > 10 and ref["failed"].max() == 0.0
+
+
+def test_f64_variants_and_blocks(module, oracle_lib):
+    """Every register-budget variant and block size gives the same bits."""
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    base = sg.air_cells(300, seed=5)
+    ref = base.copy()
+    oracle_run(oracle_lib, ref, 2.0)
+    for kind in (0, 1):
+        for block in (32, 64, 128):
+            for variant in (0, 1):
+                module.set_tuning(kind=kind, block=block, variant=variant)
+                z = base.copy()
+                module.integrate(z, 2.0, precision=0)
+                assert_bits(z, ref)
+    module.set_tuning()
+
+
+def test_f32_delta_bit_identical(module, oracle_lib):
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    for kind in (0, 1):
+        module.set_tuning(kind=kind)
+        z = sg.air_cells(512, seed=3)
+        ref = z.copy()
+        module.integrate(z, 1.0, precision=1)
+        oracle_run(oracle_lib, ref, 1.0, precision=1)
+        assert_bits(z, ref)
+    module.set_tuning()
+
+
+@pytest.mark.parametrize("method", ["ros2", "ros3"])
+def test_table_path_other_methods(module, oracle_lib, method):
+    """Non-Rodas3 methods run the table-driven kernels (TMA-staged tables)."""
+    module.set_mech(sg.Model.air().kinmech(), sg.method(method), sg.control())
+    for prec in (0, 1):
+        z = sg.air_cells(256, seed=9)
+        ref = z.copy()
+        module.integrate(z, 0.5, precision=prec)
+        oracle_run(oracle_lib, ref, 0.5, precision=prec, method=method)
+        assert_bits(z, ref)
+
+
+def test_table_path_robertson(module, oracle_lib):
+    """A mechanism other than the shipped one (Robertson) on the table path."""
+    O = oracle_lib
+    m = sg.Model.new()
+    om = O.Mechanism()
+    for name in ("A", "B", "C"):
+        m.add_species(name, True)
+        om.add_species(name, True)
+    for eq, k in (("A -> B", 0.04), ("B + B -> C + B", 3.0e7), ("B + C -> A + C", 1.0e4)):
+        m.add_reaction(eq, "arr", (k, 0.0, 0.0))
+        om.add_reaction(eq, "arr", (k, 0.0, 0.0))
+    m.finalize()
+    om.finalize()
+    ctl = sg.control(rtol=1e-6, atol=1e-12, h_min=0.0, h_start=1e-6, max_steps=100000)
+    octl = O.control(rtol=1e-6, atol=1e-12, h_min=0.0, h_start=1e-6, max_steps=100000)
+    for meth in ("ros2", "ros3", "rodas3"):
+        module.set_mech(m.kinmech(), sg.method(meth), ctl)
+        z = sg.ZoneBlock(3, 3, 64)
+        z["y"][0] = 1.0
+        z["k"][:] = np.array([0.04, 3.0e7, 1.0e4])[:, None]
+        ref = z.copy()
+        module.integrate(z, 40.0, precision=0)
+        oracle_run(O, ref, 40.0, method=meth, ctl=octl, mech=om)
+        assert_bits(z, ref)
+        golden = np.array([0.7158270687193267, 9.185534764557338e-06, 0.2841637457458339])
+        assert np.all(np.abs(z["y"][:, 0] - golden) / golden < 1e-4)
+
+
+@pytest.mark.parametrize("pulsed", [True, False], ids=["pulsed", "averaged"])
+def test_dbd_zones_multistep(module, oracle_lib, pulsed):
+    """The reference's own GPU test set-up (test_kinetics.cpp:214-227, 1092-1146):
+    zones at varied operating points, 1 ms master steps with discharge pulses or
+    the averaged source, uploads every step; GPU and oracle stay bit-identical."""
+    ctl = sg.control(rtol=1e-3, atol=1e8, h_min=1e-14, h_start=1e-9, max_steps=20000)
+    octl = oracle_lib.control(rtol=1e-3, atol=1e8, h_min=1e-14, h_start=1e-9, max_steps=20000)
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), ctl)
+    n = 24
+    i = np.arange(n)
+    args = (300.0 + 10.0 * (i % 5), 0.005 * (i % 7), 0.05 + 0.1 * (i % 3), 5000.0 + 2500.0 * (i % 4))
+    for prec in (0, 1):
+        a = sg.dbd_zones(n, *args)
+        b = sg.dbd_zones(n, *args)
+        for step in range(5):
+            t0, t1 = step * 1e-3, (step + 1) * 1e-3
+            sg.dbd_prepare_source(a, pulsed, t0, t1)
+            sg.dbd_prepare_source(b, pulsed, t0, t1)
+            module.integrate(a, t1 - t0, precision=prec)
+            oracle_run(oracle_lib, b, t1 - t0, precision=prec, ctl=octl)
+            sg.dbd_commit_pulses(a)
+            sg.dbd_commit_pulses(b)
+            assert_bits(a, b)
+        if pulsed:
+            assert a["pulses"].min() > 0
+
+
+def test_lane_count_subset(module, oracle_lib):
+    """lane_count < padded integrates only [0, lane_count); the rest is untouched."""
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    z = sg.air_cells(200, seed=21)
+    before = z.copy()
+    base = module.upload(z)
+    module.advance(z.launch(base, 0, 0.25, lane_count=77))
+    module.download(z, base)
+    ref = before.copy()
+    oracle_lib.Mechanism.air().advance("rodas3", oracle_lib.control(), ref.as_dict(), ref.padded, 0, 77, 0.25, 0, 0)
+    assert_bits(z, ref)
+    assert np.array_equal(z["y"][:, 77:], before["y"][:, 77:])
+
+
+def test_async_advance_matches(module, oracle_lib):
+    """gpu_kin_advance_async / gpu_kin_wait (the hybrid path's calls) on a page-locked block."""
+    L = sg.lib()
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    z = sg.air_cells(256, seed=4)
+    ref = z.copy()
+    dev = module.alloc(z.nbytes)
+    sg.check(L.gpu_host_register(z.data.ctypes.data, z.nbytes), "register")
+    launch = z.launch(dev, 0, 0.5, lane_count=128)
+    sg.check(L.gpu_kin_advance_async(C.byref(launch), z.data.ctypes.data, dev, z.rows, z.mutable_rows), "async")
+    kms, tms = C.c_float(), C.c_float()
+    sg.check(L.gpu_kin_wait(C.byref(kms), C.byref(tms)), "wait")
+    sg.check(L.gpu_host_unregister(z.data.ctypes.data), "unregister")
+    oracle_lib.Mechanism.air().advance("rodas3", oracle_lib.control(), ref.as_dict(), ref.padded, 0, 128, 0.5, 0, 0)
+    assert_bits(z, ref)
+    assert tms.value >= kms.value > 0.0
+
+
+def test_failed_lanes_max_steps(module, oracle_lib):
+    """Lanes that exceed max_steps are flagged failed with their last accepted state,
+    exactly as the oracle flags them; the flag is sticky on the next call."""
+    ctl = sg.control(max_steps=40)
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), ctl)
+    z = sg.air_cells(256, seed=2)
+    ref = z.copy()
+    module.integrate(z, 1.0, precision=0)
+    oracle_run(oracle_lib, ref, 1.0, ctl=oracle_lib.control(max_steps=40))
+    assert_bits(z, ref)
+    assert z["failed"].sum() > 0
+    module.integrate(z, 1.0, precision=0)
+    oracle_run(oracle_lib, ref, 1.0, ctl=oracle_lib.control(max_steps=40))
+    assert_bits(z, ref)
+
+
+def test_mixed_precision_accuracy(module, oracle_lib):
+    """Mixed path vs the FP64 oracle. Relative error per species, floored at
+    atol: |a - b| / max(|b|, atol). Bound: 1e-3 max (rtol 1e-4 with accept/reject
+    decisions that can differ near err = 1), and report the p99."""
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    z = sg.air_cells(2048, seed=1)
+    ref = z.copy()
+    module.integrate(z, 1.0, precision=2)
+    oracle_run(oracle_lib, ref, 1.0)
+    atol = sg.ATOL_1E12_MOLAR
+    err = np.abs(z["y"] - ref["y"]) / np.maximum(np.abs(ref["y"]), atol)
+    assert np.isfinite(err).all() and z["failed"].max() == 0.0
+    assert err.max() < 1e-3, (err.max(), np.quantile(err, 0.99))
+    assert np.quantile(err, 0.99) < 1e-5
+
+
+def test_invalid_inputs_rejected(module):
+    """Bad launches and mechanisms return CUDA error codes, never fault."""
+    L = sg.lib()
+    km = sg.Model.air().kinmech()
+    bad = sg.KinMech.from_buffer_copy(km)
+    bad.lu_sub[0].ij = 9999
+    assert L.gpu_kin_set_mech(C.byref(bad), C.byref(sg.method()), C.byref(sg.control())) != 0
+    module.set_mech(km)
+    z = sg.air_cells(64, seed=1)
+    launch = z.launch(0, 0, 1.0)
+    ms = C.c_float()
+    assert L.gpu_kin_advance(C.byref(launch), C.byref(ms)) != 0   # null device pointers
+    launch = z.launch(module.alloc(z.nbytes), 3, 1.0)
+    assert L.gpu_kin_advance(C.byref(launch), C.byref(ms)) != 0   # unknown precision
+
+
+def test_zero_duration_and_empty(module, oracle_lib):
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    z = sg.air_cells(64, seed=8)
+    ref = z.copy()
+    module.integrate(z, 0.0, precision=0)
+    oracle_run(oracle_lib, ref, 0.0)
+    assert_bits(z, ref)
