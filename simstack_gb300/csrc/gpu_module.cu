@@ -138,6 +138,7 @@ cudaError_t check_launch(const GpuKinLaunch *L) {
     if (!g.have_mech) return cudaErrorInvalidValue;
     if (!L || L->precision > 2 || L->padded == 0) return cudaErrorInvalidValue;
     if (L->lane_count > L->padded) return cudaErrorInvalidValue;
+    if (!(L->duration >= 0.0) || L->duration > 1.0e300) return cudaErrorInvalidValue;   // NaN, negative or infinite
     if (!L->y || !L->h || !L->steps || !L->rejects || !L->pulses || !L->failed || !L->k || !L->src || !L->pulse ||
         !L->period || !L->pulse_first || !L->pulse_count)
         return cudaErrorInvalidValue;

@@ -263,11 +263,12 @@ struct Lane {
     }
 
     // Runs the cheap transitions until the lane needs a step attempt (true)
-    // or has finished its cell (false). The transition guard only ends cells
-    // whose pulse schedule cannot terminate (non-finite counts).
+    // or has finished its cell (false). The transition guard (2^24 segment
+    // transitions per cell, far above any real pulse schedule) ends cells whose
+    // schedule cannot terminate (a non-finite pulse count), marking them failed.
     __device__ __forceinline__ bool settle(const DevArgs &A, uint32_t cell) {
         for (;;) {
-            if (++transitions > (1u << 30)) {
+            if (++transitions > (1u << 24)) {
                 failed = (T)1.0;
                 phase = kPhaseDone;
             }
