@@ -820,6 +820,196 @@ static void advance_range(const Mechanism *m, const Method *me, const Control *c
 }
 
 // ---------------------------------------------------------------------------
+// Model of this module's MIXED-precision attempt (not a reference algorithm:
+// the reference has no mixed path). FP32 RHS / -J / LU; every stage solve
+// refined by `sweeps` iterative-refinement sweeps with an FP64 residual
+// r = b - (ghinv x + (-J) x); optional diagonal scaling of the FP32 system by
+// d_i = rtol |y_i| + atol (rows by 1/d_i, columns by d_j); FP64 state, stage
+// combination, error estimate and controller -- the same controller code as
+// the FP64 lane above. The GPU's mixed kernel performs these operations in
+// this order, so the tests can compare it bit for bit.
+
+struct MixedOptions {
+    u32 sweeps;
+    u32 scaled;
+    u32 fun64;   // research switch: RHS in FP64 (k, src, y in FP64); 0 in the module's path
+};
+
+struct MixedWork {
+    std::vector<float> a, js, f32, c32, x32, d32, id32;
+    std::vector<double> ytmp, kst, b, r, f64v;
+    const double *k64 = nullptr, *src64 = nullptr;
+    void size(const Mechanism &m) {
+        f64v.resize(m.n());
+        a.resize(m.nnz ? m.nnz : 1);
+        js.resize(m.nnz ? m.nnz : 1);
+        f32.resize(m.n()); c32.resize(m.n()); x32.resize(m.n()); d32.resize(m.n()); id32.resize(m.n());
+        ytmp.resize(m.n()); kst.resize((size_t)4 * m.n()); b.resize(m.n()); r.resize(m.n());
+    }
+};
+
+// r = b - ghinv x - (-J) x over the J pattern in row order: diagonal, lower (ascending col), upper (descending col).
+static void residual64(const Mechanism &m, const float *js, double ghinv, const double *b, const double *x, double *r) {
+    for (u32 i = 0; i < m.n(); ++i) {
+        double acc = std::fma(-ghinv, x[i], b[i]);
+        acc = std::fma(-(double)js[m.diag[i]], x[i], acc);
+        for (u32 e = m.lower_begin[i]; e < m.lower_begin[i + 1]; ++e) acc = std::fma(-(double)js[m.lower[e].index], x[m.lower[e].col], acc);
+        for (u32 e = m.upper_begin[i]; e < m.upper_begin[i + 1]; ++e) acc = std::fma(-(double)js[m.upper[e].index], x[m.upper[e].col], acc);
+        r[i] = acc;
+    }
+}
+
+static void integrate_mixed(const Mechanism &m, const Method &me, const Control &ctl, const MixedOptions &opt,
+                            const float *k32, const float *src32, double *y, double &t, double t_end, double &h,
+                            Stats<double> &st, MixedWork &w) {
+    const u32 n = m.n();
+    const double zero = 0.0, one = 1.0, h_min = ctl.h_min, rtol = ctl.rtol, atol = ctl.atol;
+    const double inv_n = 1.0 / (double)n;
+    const float rtol32 = (float)ctl.rtol, atol32 = (float)ctl.atol;
+    float *a = w.a.data(), *js = w.js.data(), *f32 = w.f32.data(), *c32 = w.c32.data(), *x32 = w.x32.data();
+    float *d32 = w.d32.data(), *id32 = w.id32.data();
+    double *ytmp = w.ytmp.data(), *b = w.b.data(), *rr = w.r.data();
+    double *K[4] = {w.kst.data(), w.kst.data() + n, w.kst.data() + 2 * n, w.kst.data() + 3 * n};
+
+    bool active = t < t_end && !(st.failed > zero);
+    bool reject_last = false, reject_more = false;
+    h = h > zero ? h : ctl.h_start;
+    u32 iterations = 0;
+    while (active) {
+        if (++iterations > ctl.max_steps) { st.failed = one; break; }
+        double remaining = t_end - t;
+        double h_cap = remaining;
+        if (ctl.h_max > 0.0) h_cap = vmin(h_cap, ctl.h_max);
+        double h_wanted = vmax(h, h_min);
+        bool last = h_wanted >= remaining;
+        double hs = last ? remaining : vmin(h_wanted, h_cap);
+
+        for (u32 s = 0; s < n; ++s) c32[s] = (float)y[s];
+        if (opt.fun64) {
+            eval_fun(m, w.k64, w.src64, y, w.f64v.data());
+        } else {
+            eval_fun(m, k32, src32, c32, f32);
+        }
+        eval_neg_jac(m, k32, c32, a);
+        for (u32 i = 0; i < m.nnz; ++i) js[i] = a[i];
+        if (opt.scaled) {
+            for (u32 s = 0; s < n; ++s) {
+                d32[s] = std::fma(rtol32, vabs(c32[s]), atol32);
+                id32[s] = 1.0f / d32[s];
+            }
+            for (u32 i = 0; i < n; ++i) {
+                for (u32 e = m.lower_begin[i]; e < m.lower_begin[i + 1]; ++e) a[m.lower[e].index] = a[m.lower[e].index] * (d32[m.lower[e].col] * id32[i]);
+                for (u32 e = m.upper_begin[i]; e < m.upper_begin[i + 1]; ++e) a[m.upper[e].index] = a[m.upper[e].index] * (d32[m.upper[e].col] * id32[i]);
+            }
+        }
+        double ghinv = one / (hs * me.gamma0);
+        factor(m, (float)ghinv, a);
+        double hinv = one / hs;
+
+        for (u32 stg = 0; stg < me.stages; ++stg) {
+            u32 packed = stg * (stg - 1) / 2;
+            if (stg > 0 && me.new_f[stg]) {
+                for (u32 s = 0; s < n; ++s) ytmp[s] = y[s];
+                for (u32 j = 0; j < stg; ++j) {
+                    double av = me.a[packed + j];
+                    if (av == 0.0) continue;
+                    for (u32 s = 0; s < n; ++s) ytmp[s] = std::fma(av, K[j][s], ytmp[s]);
+                }
+                for (u32 s = 0; s < n; ++s) c32[s] = (float)ytmp[s];
+                if (opt.fun64) eval_fun(m, w.k64, w.src64, ytmp, w.f64v.data());
+                else eval_fun(m, k32, src32, c32, f32);
+            }
+            for (u32 s = 0; s < n; ++s) K[stg][s] = opt.fun64 ? w.f64v[s] : (double)f32[s];
+            for (u32 j = 0; j < stg; ++j) {
+                double c = me.c[packed + j];
+                if (c == 0.0) continue;
+                double hc = c * hinv;
+                for (u32 s = 0; s < n; ++s) K[stg][s] = std::fma(hc, K[j][s], K[stg][s]);
+            }
+            // refined solve: b in K[stg] -> x in K[stg]
+            double *x = K[stg];
+            for (u32 s = 0; s < n; ++s) b[s] = x[s];
+            for (u32 s = 0; s < n; ++s) x32[s] = opt.scaled ? (float)b[s] * id32[s] : (float)b[s];
+            solve(m, a, x32);
+            for (u32 s = 0; s < n; ++s) x[s] = opt.scaled ? (double)(x32[s] * d32[s]) : (double)x32[s];
+            for (u32 sw = 0; sw < opt.sweeps; ++sw) {
+                residual64(m, js, ghinv, b, x, rr);
+                for (u32 s = 0; s < n; ++s) x32[s] = opt.scaled ? (float)rr[s] * id32[s] : (float)rr[s];
+                solve(m, a, x32);
+                for (u32 s = 0; s < n; ++s) x[s] = x[s] + (opt.scaled ? (double)(x32[s] * d32[s]) : (double)x32[s]);
+            }
+        }
+
+        double err = zero;
+        for (u32 s = 0; s < n; ++s) {
+            double ynew = y[s], yerr = zero;
+            for (u32 stg = 0; stg < me.stages; ++stg) {
+                if (me.m[stg] != 0.0) ynew = std::fma(me.m[stg], K[stg][s], ynew);
+                if (me.e[stg] != 0.0) yerr = std::fma(me.e[stg], K[stg][s], yerr);
+            }
+            double scale = std::fma(rtol, vmax(vabs(y[s]), vabs(ynew)), atol);
+            double q = yerr / scale;
+            err = std::fma(q, q, err);
+            ytmp[s] = ynew;
+        }
+        err = vsqrt(err * inv_n);
+        if (!finite(err)) err = 1e10;
+        double fac = step_factor(err, me.order);
+        bool ok = err <= one || hs <= h_min;
+        if (ctl.fixed_step) { ok = true; fac = one; }
+        if (ok) {
+            for (u32 s = 0; s < n; ++s) {
+                double ynew = ytmp[s];
+                if (ctl.clamp_negative) ynew = vmax(ynew, zero);
+                y[s] = ynew;
+            }
+            t = last ? t_end : t + hs;
+        }
+        double h_acc = hs * fac;
+        h_acc = reject_last ? vmin(h_acc, hs) : h_acc;
+        h_acc = (last && fac >= one) ? vmax(h_acc, h_wanted) : h_acc;
+        double h_rej = reject_more ? hs * 0.1 : vmin(hs * fac, hs);
+        if (ctl.fixed_step) { h_acc = h_wanted; h_rej = h_wanted; }
+        h = ok ? h_acc : h_rej;
+        reject_more = !ok && reject_last;
+        reject_last = !ok;
+        st.steps = st.steps + (ok ? one : zero);
+        st.rejects = st.rejects + (ok ? zero : one);
+        active = t < t_end && !(st.failed > zero);
+    }
+}
+
+// Lanes [begin, end) without pulses (the mixed model covers continuous sources only).
+static void advance_mixed_range(const Mechanism *m, const Method *me, const Control *ctl, const MixedOptions *opt,
+                                const LaneArrays *a, u32 begin, u32 end, double duration) {
+    MixedWork w;
+    w.size(*m);
+    const u32 n = m->n(), R = m->R(), p = a->padded;
+    std::vector<double> y(n);
+    std::vector<float> k32(R ? R : 1), src32(n);
+    std::vector<double> k64(R ? R : 1), src64(n);
+    w.k64 = k64.data();
+    w.src64 = src64.data();
+    for (u32 i = begin; i < end; ++i) {
+        for (u32 s = 0; s < n; ++s) src64[s] = a->src[(size_t)s * p + i];
+        for (u32 r = 0; r < R; ++r) k64[r] = a->k[(size_t)r * p + i];
+        for (u32 s = 0; s < n; ++s) {
+            y[s] = a->y[(size_t)s * p + i];
+            src32[s] = (float)a->src[(size_t)s * p + i];
+        }
+        for (u32 r = 0; r < R; ++r) k32[r] = (float)a->k[(size_t)r * p + i];
+        double h = a->h[i], t = 0.0;
+        Stats<double> st = {0.0, 0.0, 0.0, a->failed[i]};
+        integrate_mixed(*m, *me, *ctl, *opt, k32.data(), src32.data(), y.data(), t, duration, h, st, w);
+        for (u32 s = 0; s < n; ++s) a->y[(size_t)s * p + i] = y[s];
+        a->h[i] = h;
+        a->failed[i] = st.failed;
+        a->steps[i] += st.steps;
+        a->rejects[i] += st.rejects;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Discharge source (air_mech.cpp:184-276): per-second (averaged) or per-pulse
 // species change for energy_J_cm3 deposited into gas y at temperature T.
 
@@ -1031,6 +1221,32 @@ s32 or_advance(void *h, s32 method_id, const Control *ctl, const LaneArrays *arr
                 if (c >= nchunk) break;
                 u32 b = begin + c * per, e = std::min(end, b + per);
                 run(b, e);
+            }
+        });
+    for (auto &t : pool) t.join();
+    return 0;
+}
+
+// Model of the module's mixed-precision path (see integrate_mixed), lanes [begin, end).
+s32 or_advance_mixed(void *h, s32 method_id, const Control *ctl, const LaneArrays *arrays, u32 begin, u32 end,
+                     double duration, u32 sweeps, u32 scaled, u32 threads) {
+    Mechanism *m = (Mechanism *)h;
+    Method me = method_coefficients(method_id);
+    MixedOptions opt = {sweeps & 0xFF, scaled, (sweeps >> 8) & 1};
+    if (threads == 0) threads = std::thread::hardware_concurrency();
+    if (threads == 0) threads = 1;
+    if (end <= begin) return 0;
+    u32 lanes = end - begin, chunks = std::min<u32>(lanes, 4 * threads), per = (lanes + chunks - 1) / chunks;
+    u32 nchunk = (lanes + per - 1) / per;
+    std::atomic<u32> cursor(0);
+    std::vector<std::thread> pool;
+    for (u32 tI = 0; tI < std::min(threads, nchunk); ++tI)
+        pool.emplace_back([&]() {
+            for (;;) {
+                u32 c = cursor.fetch_add(1);
+                if (c >= nchunk) break;
+                u32 b = begin + c * per, e = std::min(end, b + per);
+                advance_mixed_range(m, &me, ctl, &opt, arrays, b, e, duration);
             }
         });
     for (auto &t : pool) t.join();

@@ -112,6 +112,8 @@ def lib() -> C.CDLL:
         L.or_integrate_f64.restype = i32
         L.or_advance.argtypes = [vp, i32, C.POINTER(Control), C.POINTER(LaneArrays), u32, u32, d, u32, u32]
         L.or_advance.restype = i32
+        L.or_advance_mixed.argtypes = [vp, i32, C.POINTER(Control), C.POINTER(LaneArrays), u32, u32, d, u32, u32, u32]
+        L.or_advance_mixed.restype = i32
         L.or_source_delta.argtypes = [vp, u32, d, d, vp]
         L.or_advect.argtypes = [vp, u32, u32, u32, vp, d, u32]
         L.or_fnv1a.argtypes = [vp, u64]
@@ -218,6 +220,17 @@ class Mechanism:
                               threads)
         if rc != 0:
             raise RuntimeError(f"or_advance failed: {rc}")
+
+
+def advance_mixed(mech: "Mechanism", method: str, ctl: Control, block: dict, padded: int, begin: int, end: int,
+                  duration: float, sweeps: int = 1, scaled: int = 1, threads: int = 0) -> None:
+    """Model of the GPU module's mixed-precision path (FP32 chemistry, FP64 residual,
+    state and control); used to check the GPU's mixed kernel bit for bit."""
+    la = lane_arrays(block, padded)
+    rc = lib().or_advance_mixed(mech.h, METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, sweeps,
+                                scaled, threads)
+    if rc != 0:
+        raise RuntimeError(f"or_advance_mixed failed: {rc}")
 
 
 def source_delta(y: np.ndarray, energy_J_cm3: float, T_K: float) -> np.ndarray:

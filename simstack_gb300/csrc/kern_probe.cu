@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256) probe_kernel(double *out, uint32_t iters)
 #pragma unroll
             for (int j = 0; j < 8; ++j) {
                 double d = (double)a[j];
-                a[j] = (float)(d * 0.5) * 2.0f;
+                a[j] = __int_as_float(__double2hiint(d) ^ (int)j) ;
             }
         }
         float s = 0.0f;
