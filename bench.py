@@ -324,7 +324,12 @@ def run_ours(args):
     zm = z.copy()
     mod.download(zm, work)
     atol = sg.ATOL_1E12_MOLAR
-    rel = np.abs(zm["y"][:, :cells] - zc["y"][:, :cells]) / np.maximum(np.abs(zc["y"][:, :cells]), atol)
+    ya, yb = zm["y"][:, :cells], zc["y"][:, :cells]
+    rel = np.abs(ya - yb) / np.maximum(np.abs(yb), atol)
+    sig_mask = yb >= 1e-12 * yb.sum(axis=0)
+    with np.errstate(all="ignore"):
+        rel_sig = (np.abs(ya - yb) / np.abs(yb))[sig_mask]
+    flips = float(np.mean((zm["steps"][:cells] != zc["steps"][:cells]) | (zm["rejects"][:cells] != zc["rejects"][:cells])))
 
     # end-to-end through the C ABI with host buffers (pinned), per step
     sg.check(L.gpu_host_register(z.data.ctypes.data, z.nbytes), "gpu_host_register")
@@ -392,8 +397,12 @@ def run_ours(args):
         "fp64": {"value": v64, "ms_per_step": ms_step64, "kernel_ms": ms64,
                  "parity": "bit-identical to the reference CPU solver (tests/test_gpu_parity.py)"},
         "mixed": {"value": vmx, "ms_per_step": ms_stepmx, "kernel_ms": msmx, "speedup_vs_fp64": v64 and vmx / v64,
-                  "rel_err_vs_fp64_max": float(rel.max()), "rel_err_vs_fp64_p99": float(np.quantile(rel, 0.99)),
-                  "rel_err_definition": "|a-b| / max(|b|, atol) per species over all cells"},
+                  "rel_err_vs_fp64": {"max": float(rel_sig.max()), "p99": float(np.quantile(rel_sig, 0.99)),
+                                      "definition": "|a-b|/|b| over species >= 1e-6 ppm of the cell total, all cells"},
+                  "rel_err_vs_fp64_atol_floored": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+                                                   "definition": "|a-b|/max(|b|, atol) over every species and cell"},
+                  "cells_with_different_step_counts": flips,
+                  "reference_for_errors": "the FP64 path on the same batch, bit-identical to the reference CPU solver"},
         "steps_per_cell": {"mean": steps_total / cells, "failed_cells": failed},
         "roofline": {"bound": "fp64", "achieved": ach64 if head == "f64" else achmx, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": (ach64 if head == "f64" else achmx) / fp64_peak,

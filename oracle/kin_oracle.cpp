@@ -90,7 +90,9 @@ struct Mechanism {
     std::vector<LuPivot> pivots;
     std::vector<LuUpdate> updates;
     std::vector<RowEntry> lower, upper;
-    std::vector<u8> pattern;   // n*n, after fill-in
+    std::vector<u8> pattern;       // n*n, after fill-in
+    std::vector<u8> jac_pattern;   // n*n, J + diagonal before fill-in
+    std::vector<u32> slot;         // n*n -> compact index (or ~0u)
     bool failed = false;
     std::string error;
     u32 n() const { return (u32)names.size(); }
@@ -208,6 +210,7 @@ static void finalize(Mechanism *m) {
     for (const Reaction &rx : m->reactions)
         for (u32 p = 0; p < rx.reactant_count; ++p)
             for (u32 e = 0; e < rx.net_count; ++e) pat[(size_t)rx.net_species[e] * n + rx.reactant[p]] = 1;
+    m->jac_pattern = pat;
     for (u32 i = 1; i < n; ++i)
         for (u32 k = 0; k < i; ++k)
             if (pat[(size_t)i * n + k])
@@ -219,6 +222,7 @@ static void finalize(Mechanism *m) {
     for (u32 i = 0; i < n; ++i)
         for (u32 j = 0; j < n; ++j)
             if (pat[(size_t)i * n + j]) index[(size_t)i * n + j] = m->nnz++;
+    m->slot = index;
     m->diag.resize(n);
     for (u32 i = 0; i < n; ++i) m->diag[i] = index[(size_t)i * n + i];
 
@@ -821,55 +825,98 @@ static void advance_range(const Mechanism *m, const Method *me, const Control *c
 
 // ---------------------------------------------------------------------------
 // Model of this module's MIXED-precision attempt (not a reference algorithm:
-// the reference has no mixed path). FP32 RHS / -J / LU; every stage solve
-// refined by `sweeps` iterative-refinement sweeps with an FP64 residual
-// r = b - (ghinv x + (-J) x); optional diagonal scaling of the FP32 system by
-// d_i = rtol |y_i| + atol (rows by 1/d_i, columns by d_j); FP64 state, stage
-// combination, error estimate and controller -- the same controller code as
-// the FP64 lane above. The GPU's mixed kernel performs these operations in
-// this order, so the tests can compare it bit for bit.
+// the reference has no mixed path), in the GPU kernel's operation order so
+// the tests can compare the GPU's mixed kernel with it bit for bit:
+//   RHS      double-float (hi + lo FP32 pairs) at the FP64 stage point
+//   -J, LU   FP32 at the FP32 rounding of the point
+//   solve    FP32 LU solve, then `sweeps` refinement sweeps with the FP64
+//            residual r = b - ghinv x - (-J) x over the Jacobian pattern
+//   state, stage combination, error estimate, controller: FP64, the same
+//            controller code as the FP64 lane above.
 
-struct MixedOptions {
-    u32 sweeps;
-    u32 scaled;
-    u32 fun64;   // research switch: RHS in FP64 (k, src, y in FP64); 0 in the module's path
+struct Df2 {
+    float hi, lo;
 };
+static inline Df2 df_from(double d) {
+    float h = (float)d;
+    return Df2{h, (float)(d - (double)h)};
+}
+static inline double df_to(Df2 a) { return (double)a.hi + (double)a.lo; }
+static inline Df2 df_mul(Df2 a, Df2 b) {
+    float p = a.hi * b.hi;
+    float e = std::fma(a.hi, b.hi, -p);
+    e = std::fma(a.hi, b.lo, e);
+    e = std::fma(a.lo, b.hi, e);
+    float s = p + e;
+    return Df2{s, e - (s - p)};
+}
+static inline Df2 df_add(Df2 a, Df2 b) {
+    float s = a.hi + b.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e = e + a.lo;
+    e = e + b.lo;
+    float t = s + e;
+    return Df2{t, e - (t - s)};
+}
+static inline Df2 df_scale(Df2 a, float c) { return Df2{a.hi * c, a.lo * c}; }
+
+static void eval_fun_df(const Mechanism &m, const Df2 *k, const Df2 *src, const Df2 *y, Df2 *f) {
+    for (u32 s = 0; s < m.n(); ++s) f[s] = src[s];
+    for (u32 r = 0; r < m.R(); ++r) {
+        const Reaction &rx = m.reactions[r];
+        Df2 rate = k[r];
+        for (u32 p = 0; p < rx.reactant_count; ++p) rate = df_mul(rate, y[rx.reactant[p]]);
+        for (u32 e = 0; e < rx.net_count; ++e) {
+            const int c = rx.net_coef[e];
+            Df2 term = c == 1 ? rate
+                       : (c == -1 || c == 2 || c == -2 || c == 4 || c == -4) ? df_scale(rate, (float)c)
+                                                                              : df_mul(rate, Df2{(float)c, 0.0f});
+            f[rx.net_species[e]] = df_add(f[rx.net_species[e]], term);
+        }
+    }
+}
 
 struct MixedWork {
-    std::vector<float> a, js, f32, c32, x32, d32, id32;
-    std::vector<double> ytmp, kst, b, r, f64v;
-    const double *k64 = nullptr, *src64 = nullptr;
+    std::vector<float> a, js, k32, x32;
+    std::vector<Df2> kd, sd, yd, fd;
+    std::vector<double> ytmp, kst, b, r;
     void size(const Mechanism &m) {
-        f64v.resize(m.n());
         a.resize(m.nnz ? m.nnz : 1);
         js.resize(m.nnz ? m.nnz : 1);
-        f32.resize(m.n()); c32.resize(m.n()); x32.resize(m.n()); d32.resize(m.n()); id32.resize(m.n());
+        k32.resize(m.R() ? m.R() : 1);
+        x32.resize(m.n());
+        kd.resize(m.R() ? m.R() : 1);
+        sd.resize(m.n()); yd.resize(m.n()); fd.resize(m.n());
         ytmp.resize(m.n()); kst.resize((size_t)4 * m.n()); b.resize(m.n()); r.resize(m.n());
     }
 };
 
-// r = b - ghinv x - (-J) x over the J pattern in row order: diagonal, lower (ascending col), upper (descending col).
+// r = b - ghinv x - (-J) x over each row's Jacobian-pattern entries, ascending column.
 static void residual64(const Mechanism &m, const float *js, double ghinv, const double *b, const double *x, double *r) {
-    for (u32 i = 0; i < m.n(); ++i) {
+    const u32 n = m.n();
+    for (u32 i = 0; i < n; ++i) {
         double acc = std::fma(-ghinv, x[i], b[i]);
-        acc = std::fma(-(double)js[m.diag[i]], x[i], acc);
-        for (u32 e = m.lower_begin[i]; e < m.lower_begin[i + 1]; ++e) acc = std::fma(-(double)js[m.lower[e].index], x[m.lower[e].col], acc);
-        for (u32 e = m.upper_begin[i]; e < m.upper_begin[i + 1]; ++e) acc = std::fma(-(double)js[m.upper[e].index], x[m.upper[e].col], acc);
+        for (u32 j = 0; j < n; ++j)
+            if (m.jac_pattern[(size_t)i * n + j]) acc = std::fma(-(double)js[m.slot[(size_t)i * n + j]], x[j], acc);
         r[i] = acc;
     }
 }
 
-static void integrate_mixed(const Mechanism &m, const Method &me, const Control &ctl, const MixedOptions &opt,
-                            const float *k32, const float *src32, double *y, double &t, double t_end, double &h,
-                            Stats<double> &st, MixedWork &w) {
+static void integrate_mixed(const Mechanism &m, const Method &me, const Control &ctl, u32 sweeps, double *y, double &t,
+                            double t_end, double &h, Stats<double> &st, MixedWork &w) {
     const u32 n = m.n();
     const double zero = 0.0, one = 1.0, h_min = ctl.h_min, rtol = ctl.rtol, atol = ctl.atol;
     const double inv_n = 1.0 / (double)n;
-    const float rtol32 = (float)ctl.rtol, atol32 = (float)ctl.atol;
-    float *a = w.a.data(), *js = w.js.data(), *f32 = w.f32.data(), *c32 = w.c32.data(), *x32 = w.x32.data();
-    float *d32 = w.d32.data(), *id32 = w.id32.data();
+    float *a = w.a.data(), *js = w.js.data(), *x32 = w.x32.data();
     double *ytmp = w.ytmp.data(), *b = w.b.data(), *rr = w.r.data();
     double *K[4] = {w.kst.data(), w.kst.data() + n, w.kst.data() + 2 * n, w.kst.data() + 3 * n};
+    std::vector<float> yhi(n);
+
+    auto rhs = [&](const double *yy) {
+        for (u32 s = 0; s < n; ++s) w.yd[s] = df_from(yy[s]);
+        eval_fun_df(m, w.kd.data(), w.sd.data(), w.yd.data(), w.fd.data());
+    };
 
     bool active = t < t_end && !(st.failed > zero);
     bool reject_last = false, reject_more = false;
@@ -884,24 +931,10 @@ static void integrate_mixed(const Mechanism &m, const Method &me, const Control 
         bool last = h_wanted >= remaining;
         double hs = last ? remaining : vmin(h_wanted, h_cap);
 
-        for (u32 s = 0; s < n; ++s) c32[s] = (float)y[s];
-        if (opt.fun64) {
-            eval_fun(m, w.k64, w.src64, y, w.f64v.data());
-        } else {
-            eval_fun(m, k32, src32, c32, f32);
-        }
-        eval_neg_jac(m, k32, c32, a);
+        rhs(y);
+        for (u32 s = 0; s < n; ++s) yhi[s] = w.yd[s].hi;
+        eval_neg_jac(m, w.k32.data(), yhi.data(), a);
         for (u32 i = 0; i < m.nnz; ++i) js[i] = a[i];
-        if (opt.scaled) {
-            for (u32 s = 0; s < n; ++s) {
-                d32[s] = std::fma(rtol32, vabs(c32[s]), atol32);
-                id32[s] = 1.0f / d32[s];
-            }
-            for (u32 i = 0; i < n; ++i) {
-                for (u32 e = m.lower_begin[i]; e < m.lower_begin[i + 1]; ++e) a[m.lower[e].index] = a[m.lower[e].index] * (d32[m.lower[e].col] * id32[i]);
-                for (u32 e = m.upper_begin[i]; e < m.upper_begin[i + 1]; ++e) a[m.upper[e].index] = a[m.upper[e].index] * (d32[m.upper[e].col] * id32[i]);
-            }
-        }
         double ghinv = one / (hs * me.gamma0);
         factor(m, (float)ghinv, a);
         double hinv = one / hs;
@@ -915,28 +948,25 @@ static void integrate_mixed(const Mechanism &m, const Method &me, const Control 
                     if (av == 0.0) continue;
                     for (u32 s = 0; s < n; ++s) ytmp[s] = std::fma(av, K[j][s], ytmp[s]);
                 }
-                for (u32 s = 0; s < n; ++s) c32[s] = (float)ytmp[s];
-                if (opt.fun64) eval_fun(m, w.k64, w.src64, ytmp, w.f64v.data());
-                else eval_fun(m, k32, src32, c32, f32);
+                rhs(ytmp);
             }
-            for (u32 s = 0; s < n; ++s) K[stg][s] = opt.fun64 ? w.f64v[s] : (double)f32[s];
+            for (u32 s = 0; s < n; ++s) K[stg][s] = df_to(w.fd[s]);
             for (u32 j = 0; j < stg; ++j) {
                 double c = me.c[packed + j];
                 if (c == 0.0) continue;
                 double hc = c * hinv;
                 for (u32 s = 0; s < n; ++s) K[stg][s] = std::fma(hc, K[j][s], K[stg][s]);
             }
-            // refined solve: b in K[stg] -> x in K[stg]
             double *x = K[stg];
             for (u32 s = 0; s < n; ++s) b[s] = x[s];
-            for (u32 s = 0; s < n; ++s) x32[s] = opt.scaled ? (float)b[s] * id32[s] : (float)b[s];
+            for (u32 s = 0; s < n; ++s) x32[s] = (float)b[s];
             solve(m, a, x32);
-            for (u32 s = 0; s < n; ++s) x[s] = opt.scaled ? (double)(x32[s] * d32[s]) : (double)x32[s];
-            for (u32 sw = 0; sw < opt.sweeps; ++sw) {
+            for (u32 s = 0; s < n; ++s) x[s] = (double)x32[s];
+            for (u32 sw = 0; sw < sweeps; ++sw) {
                 residual64(m, js, ghinv, b, x, rr);
-                for (u32 s = 0; s < n; ++s) x32[s] = opt.scaled ? (float)rr[s] * id32[s] : (float)rr[s];
+                for (u32 s = 0; s < n; ++s) x32[s] = (float)rr[s];
                 solve(m, a, x32);
-                for (u32 s = 0; s < n; ++s) x[s] = x[s] + (opt.scaled ? (double)(x32[s] * d32[s]) : (double)x32[s]);
+                for (u32 s = 0; s < n; ++s) x[s] = x[s] + (double)x32[s];
             }
         }
 
@@ -979,34 +1009,50 @@ static void integrate_mixed(const Mechanism &m, const Method &me, const Control 
     }
 }
 
-// Lanes [begin, end) without pulses (the mixed model covers continuous sources only).
-static void advance_mixed_range(const Mechanism *m, const Method *me, const Control *ctl, const MixedOptions *opt,
+// kin_advance for the mixed model: segments between pulses, as advance() above.
+static void advance_mixed_lane(const Mechanism &m, const Method &me, const Control &ctl, u32 sweeps, const LaneArrays &a,
+                               u32 i, double duration, MixedWork &w, std::vector<double> &y) {
+    const u32 n = m.n(), R = m.R(), p = a.padded;
+    for (u32 s = 0; s < n; ++s) {
+        y[s] = a.y[(size_t)s * p + i];
+        w.sd[s] = df_from(a.src[(size_t)s * p + i]);
+    }
+    for (u32 r = 0; r < R; ++r) {
+        w.kd[r] = df_from(a.k[(size_t)r * p + i]);
+        w.k32[r] = w.kd[r].hi;
+    }
+    double h = a.h[i], per = a.period[i], first = a.pulse_first[i], count = a.pulse_count[i];
+    Stats<double> st = {0.0, 0.0, 0.0, a.failed[i]};
+    double t = 0.0, applied = 0.0;
+    for (;;) {
+        bool pending = applied < count;
+        double next_pulse = std::fma(applied, per, first);
+        double seg_end = pending ? vmin(next_pulse, duration) : duration;
+        integrate_mixed(m, me, ctl, sweeps, y.data(), t, seg_end, h, st, w);
+        bool alive = !(st.failed > 0.0);
+        bool hit = pending && alive && t >= seg_end;
+        if (hit) {
+            for (u32 s = 0; s < n; ++s) y[s] = y[s] + a.pulse[(size_t)s * p + i];
+            applied = applied + 1.0;
+            st.pulses = st.pulses + 1.0;
+            h = ctl.h_start;
+        }
+        if ((t >= duration && applied >= count) || !alive) break;
+    }
+    for (u32 s = 0; s < n; ++s) a.y[(size_t)s * p + i] = y[s];
+    a.h[i] = h;
+    a.failed[i] = st.failed;
+    a.steps[i] += st.steps;
+    a.rejects[i] += st.rejects;
+    a.pulses[i] += st.pulses;
+}
+
+static void advance_mixed_range(const Mechanism *m, const Method *me, const Control *ctl, u32 sweeps,
                                 const LaneArrays *a, u32 begin, u32 end, double duration) {
     MixedWork w;
     w.size(*m);
-    const u32 n = m->n(), R = m->R(), p = a->padded;
-    std::vector<double> y(n);
-    std::vector<float> k32(R ? R : 1), src32(n);
-    std::vector<double> k64(R ? R : 1), src64(n);
-    w.k64 = k64.data();
-    w.src64 = src64.data();
-    for (u32 i = begin; i < end; ++i) {
-        for (u32 s = 0; s < n; ++s) src64[s] = a->src[(size_t)s * p + i];
-        for (u32 r = 0; r < R; ++r) k64[r] = a->k[(size_t)r * p + i];
-        for (u32 s = 0; s < n; ++s) {
-            y[s] = a->y[(size_t)s * p + i];
-            src32[s] = (float)a->src[(size_t)s * p + i];
-        }
-        for (u32 r = 0; r < R; ++r) k32[r] = (float)a->k[(size_t)r * p + i];
-        double h = a->h[i], t = 0.0;
-        Stats<double> st = {0.0, 0.0, 0.0, a->failed[i]};
-        integrate_mixed(*m, *me, *ctl, *opt, k32.data(), src32.data(), y.data(), t, duration, h, st, w);
-        for (u32 s = 0; s < n; ++s) a->y[(size_t)s * p + i] = y[s];
-        a->h[i] = h;
-        a->failed[i] = st.failed;
-        a->steps[i] += st.steps;
-        a->rejects[i] += st.rejects;
-    }
+    std::vector<double> y(m->n());
+    for (u32 i = begin; i < end; ++i) advance_mixed_lane(*m, *me, *ctl, sweeps, *a, i, duration, w, y);
 }
 
 // ---------------------------------------------------------------------------
@@ -1232,7 +1278,7 @@ s32 or_advance_mixed(void *h, s32 method_id, const Control *ctl, const LaneArray
                      double duration, u32 sweeps, u32 scaled, u32 threads) {
     Mechanism *m = (Mechanism *)h;
     Method me = method_coefficients(method_id);
-    MixedOptions opt = {sweeps & 0xFF, scaled, (sweeps >> 8) & 1};
+    (void)scaled;
     if (threads == 0) threads = std::thread::hardware_concurrency();
     if (threads == 0) threads = 1;
     if (end <= begin) return 0;
@@ -1246,7 +1292,7 @@ s32 or_advance_mixed(void *h, s32 method_id, const Control *ctl, const LaneArray
                 u32 c = cursor.fetch_add(1);
                 if (c >= nchunk) break;
                 u32 b = begin + c * per, e = std::min(end, b + per);
-                advance_mixed_range(m, &me, ctl, &opt, arrays, b, e, duration);
+                advance_mixed_range(m, &me, ctl, sweeps, arrays, b, e, duration);
             }
         });
     for (auto &t : pool) t.join();

@@ -332,7 +332,19 @@ SGB_API int32_t gpu_kin_set_mech(const KinMech *mech, const KinMethod *method, c
         for (uint32_t e = 0; e < rx.net_count; ++e)
             if (rx.net_species[e] >= n) return (int32_t)cudaErrorInvalidValue;
     }
-    cudaError_t e = cudaMemcpyAsync(g.d_tables, mech, sizeof(KinMech), cudaMemcpyHostToDevice, g.stream);
+    // staged image: the record, then the Jacobian-pattern bitmask (slots some
+    // reaction scatters into, plus the diagonal)
+    static uint8_t image[kTableBytes];
+    memset(image, 0, sizeof(image));
+    memcpy(image, mech, sizeof(KinMech));
+    uint8_t *mask = image + kJacMaskOffset;
+    for (uint32_t i = 0; i < n; ++i) mask[mech->diag[i] >> 3] |= (uint8_t)(1u << (mech->diag[i] & 7));
+    for (uint32_t r = 0; r < mech->reaction_count; ++r) {
+        const KinReaction &rx = mech->reactions[r];
+        for (uint32_t p = 0; p < rx.reactant_count; ++p)
+            for (uint32_t e = 0; e < rx.net_count; ++e) mask[rx.jac_index[p][e] >> 3] |= (uint8_t)(1u << (rx.jac_index[p][e] & 7));
+    }
+    cudaError_t e = cudaMemcpyAsync(g.d_tables, image, kTableBytes, cudaMemcpyHostToDevice, g.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
     if (e != cudaSuccess) return (int32_t)e;
     g.mech = *mech;

@@ -61,6 +61,27 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
     }
     fprintf(f, "    }\n\n");
 
+    // fun in double-float (mixed path): the same terms in the same order as fun,
+    // each rate a double-float product, each species a double-float sum.
+    fprintf(f, "    static __device__ __forceinline__ void fun_df(const float *__restrict__ khi, const float *__restrict__ klo, const float *__restrict__ shi, const float *__restrict__ slo, const float *__restrict__ yhi, const float *__restrict__ ylo, float *__restrict__ fhi, float *__restrict__ flo) {\n");
+    fprintf(f, "        Df acc[%u];\n", n);
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        acc[%u] = Df{shi[%u], slo[%u]};\n", s, s, s);
+    for (uint32_t r = 0; r < R; ++r) {
+        const Reaction &rx = m.reactions[r];
+        fprintf(f, "        { Df rate = Df{khi[%u], klo[%u]};\n", r, r);
+        for (uint32_t q : rx.reactants) fprintf(f, "          rate = df_mul(rate, Df{yhi[%u], ylo[%u]});\n", q, q);
+        for (auto &e : rx.net) {
+            int c = e.second;
+            if (c == 1) fprintf(f, "          acc[%u] = df_add(acc[%u], rate);\n", e.first, e.first);
+            else if (c == -1 || c == 2 || c == -2 || c == 4 || c == -4)
+                fprintf(f, "          acc[%u] = df_add(acc[%u], df_scale(rate, %d.0f));\n", e.first, e.first, c);
+            else fprintf(f, "          acc[%u] = df_add(acc[%u], df_mul(rate, Df{%d.0f, 0.0f}));\n", e.first, e.first, c);
+        }
+        fprintf(f, "        }\n");
+    }
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        fhi[%u] = acc[%u].hi; flo[%u] = acc[%u].lo;\n", s, s, s, s);
+    fprintf(f, "    }\n\n");
+
     // -J into the compact LU storage
     fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void neg_jac(const T *__restrict__ k, const T *__restrict__ y, T *__restrict__ a) {\n");
     std::vector<uint8_t> written(S.nnz, 0);
@@ -125,7 +146,7 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
     for (uint32_t i = 0; i < n; ++i) {
         fprintf(f, "        { double acc = sgb_fma(-ghinv, x[%u], b[%u]);\n", i, i);
         for (size_t q = 0; q < jslots.size(); ++q)
-            if (jrow[q] == i) fprintf(f, "          acc = sgb_fma(-(double)js[%zu], x[%u], acc);\n", q, jcol[q]);
+            if (jrow[q] == i) fprintf(f, "          acc = sgb_fma(-cvt_f2d(js[%zu]), x[%u], acc);\n", q, jcol[q]);
         fprintf(f, "          r[%u] = acc; }\n", i);
     }
     fprintf(f, "    }\n");

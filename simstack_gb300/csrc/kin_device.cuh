@@ -64,6 +64,64 @@ __device__ __forceinline__ float sgb_first_neg(float d) {
     return __uint_as_float((b << 1) == 0 ? 0u : (b ^ 0x80000000u));
 }
 
+// Exact FP32 <-> FP64 conversions on the integer pipe. On GB300 the
+// hardware conversion instructions issue at the FP64 rate (measured: ~2 per
+// clock per SM), so the mixed path would spend its FP64 budget converting;
+// these produce the same bits as cvt.f64.f32 / cvt.rn.f32.f64 for normal
+// values and zeros and defer to the hardware instruction for subnormals,
+// infinities and NaNs.
+__device__ __forceinline__ double cvt_f2d(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned e = (u >> 23) & 0xFFu;
+    if (e - 1u < 254u) {
+        const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0x000FFFFFu);
+        return __hiloint2double((int)hi, (int)(u << 29));
+    }
+    if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)f;
+}
+__device__ __forceinline__ float cvt_d2f(double d) {
+    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+    const unsigned e = (hi >> 20) & 0x7FFu;
+    if (e - 897u < 254u) {   // result is a normal float (biased exponent 1..254) before rounding
+        unsigned r = ((e - 896u) << 23) | ((hi & 0x000FFFFFu) << 3) | (lo >> 29);
+        const unsigned rest = lo & 0x1FFFFFFFu, half = 0x10000000u;
+        r += (unsigned)((rest > half) | ((rest == half) & (r & 1u)));   // round to nearest even; a carry moves the exponent
+        return __uint_as_float((hi & 0x80000000u) | r);
+    }
+    if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
+    return __double2float_rn(d);
+}
+
+// Double-float arithmetic: a value is hi + lo, two FP32 numbers (~48-bit
+// significand). The mixed path evaluates the RHS this way on the FP32 pipe.
+struct Df {
+    float hi, lo;
+};
+__device__ __forceinline__ Df df_from(double d) {
+    const float h = cvt_d2f(d);
+    return Df{h, cvt_d2f(d - cvt_f2d(h))};   // d - h is exact in FP64
+}
+__device__ __forceinline__ double df_to(Df a) { return cvt_f2d(a.hi) + cvt_f2d(a.lo); }
+__device__ __forceinline__ Df df_mul(Df a, Df b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    const float s = p + e;
+    return Df{s, e - (s - p)};
+}
+__device__ __forceinline__ Df df_add(Df a, Df b) {
+    const float s = a.hi + b.hi;
+    const float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b.hi - bb);
+    e = e + a.lo;
+    e = e + b.lo;
+    const float t = s + e;
+    return Df{t, e - (t - s)};
+}
+__device__ __forceinline__ Df df_scale(Df a, float c) { return Df{a.hi * c, a.lo * c}; }   // exact for c = +-1, +-2, +-4
+
 // x^(1/3) on [1e-4, 1e4]: x^(1/4) x^(1/16) x^(1/64) from six square roots,
 // then two Newton steps; no libm (base_lane.h:123-135).
 template <class T> __device__ __forceinline__ T cbrt_clamped(T x) {
@@ -158,7 +216,8 @@ struct Lane {
     // cell data
     T y[N];
     T base[kDelta ? N : 1];
-    Cf k[R], src[N];
+    Cf k[kMixed ? 1 : R], src[kMixed ? 1 : N];
+    float khi[kMixed ? R : 1], klo[kMixed ? R : 1], shi[kMixed ? N : 1], slo[kMixed ? N : 1];   // mixed: double-float k, src
     T t, h, seg_end, applied, duration, period, first, count;
     T steps, rejects, pulses, failed;
     uint32_t iterations, transitions;
@@ -166,8 +225,9 @@ struct Lane {
     bool pending, reject_last, reject_more;
     // per-attempt scratch
     Cf lu[NNZ];
-    Cf fcn[N];
-    Cf ceval[kMixed || kDelta ? N : 1];      // f32 evaluation point (mixed) / base + increment (delta)
+    Cf fcn[kMixed ? 1 : N];
+    Cf ceval[kDelta ? N : 1];                  // delta: base + increment
+    float yhi[kMixed ? N : 1], ylo[kMixed ? N : 1], fhi[kMixed ? N : 1], flo[kMixed ? N : 1];   // mixed: double-float point, RHS
     T ytmp[N];
     T K[S][N];
     float js[kMixed ? Ops::NJ : 1];            // mixed: -J pattern entries before the factorisation
@@ -189,11 +249,23 @@ struct Lane {
             } else {
                 y[s] = (T)v;
             }
-            src[s] = (Cf)A.src[(size_t)s * p + i];
+            if constexpr (kMixed) {
+                const Df v = df_from(A.src[(size_t)s * p + i]);
+                shi[s] = v.hi;
+                slo[s] = v.lo;
+            } else {
+                src[s] = (Cf)A.src[(size_t)s * p + i];
+            }
         }
         for (int r = 0; r < R; ++r) {
             if (r >= (int)rr_) break;
-            k[r] = (Cf)A.k[(size_t)r * p + i];
+            if constexpr (kMixed) {
+                const Df v = df_from(A.k[(size_t)r * p + i]);
+                khi[r] = v.hi;
+                klo[r] = v.lo;
+            } else {
+                k[r] = (Cf)A.k[(size_t)r * p + i];
+            }
         }
         h = (T)A.h[i];
         period = (T)A.period[i];
@@ -295,15 +367,21 @@ struct Lane {
                 ceval[s] = base[s] + yy[s];
             }
             at = ceval;
-        } else if constexpr (kMixed) {
-            for (int s = 0; s < N; ++s) {
-                if (s >= (int)nn) break;
-                ceval[s] = (Cf)yy[s];
-            }
-            at = ceval;
         } else {
-            at = yy;
+            at = (const Cf *)yy;
         }
+    }
+
+    // Mixed path: the RHS at yy (FP64) in double-float on the FP32 pipe.
+    __device__ __forceinline__ void rhs_df(const double *yy) {
+        const uint32_t nn = n();
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            const Df v = df_from(yy[s]);
+            yhi[s] = v.hi;
+            ylo[s] = v.lo;
+        }
+        ops.fun_df(khi, klo, shi, slo, yhi, ylo, fhi, flo);
     }
 
     // Mixed path: x = W^-1 b with the FP32 LU, then `sweeps` refinement
@@ -312,23 +390,23 @@ struct Lane {
         const uint32_t nn = n();
         for (int s = 0; s < N; ++s) {
             if (s >= (int)nn) break;
-            x32[s] = (float)rb[s];
+            x32[s] = cvt_d2f(rb[s]);
         }
         ops.solve(lu, x32);
         for (int s = 0; s < N; ++s) {
             if (s >= (int)nn) break;
-            x[s] = (double)x32[s];
+            x[s] = cvt_f2d(x32[s]);
         }
         for (uint32_t sw = 0; sw < A.ir_sweeps; ++sw) {
             ops.residual(js, ghinv, rb, x, rr);
             for (int s = 0; s < N; ++s) {
                 if (s >= (int)nn) break;
-                x32[s] = (float)rr[s];
+                x32[s] = cvt_d2f(rr[s]);
             }
             ops.solve(lu, x32);
             for (int s = 0; s < N; ++s) {
                 if (s >= (int)nn) break;
-                x[s] = x[s] + (double)x32[s];
+                x[s] = x[s] + cvt_f2d(x32[s]);
             }
         }
     }
@@ -347,13 +425,19 @@ struct Lane {
         bool last = h_wanted >= remaining;
         T hs = last ? remaining : vmin(h_wanted, h_cap);
 
-        const Cf *at;
-        eval_point(y, at);
-        ops.fun(k, src, at, fcn);
-        ops.neg_jac(k, at, lu);
-        if constexpr (kMixed) ops.save_jac(lu, js);
+        const Cf *at = nullptr;
+        if constexpr (kMixed) {
+            rhs_df(y);
+            ops.neg_jac(khi, yhi, lu);   // FP32 Jacobian at the FP32 rounding of y
+            ops.save_jac(lu, js);
+        } else {
+            eval_point(y, at);
+            ops.fun(k, src, at, fcn);
+            ops.neg_jac(k, at, lu);
+        }
         T ghinv = one / (hs * (T)M::gamma0(A));
-        ops.factor((Cf)ghinv, lu);
+        if constexpr (kMixed) ops.factor(cvt_d2f(ghinv), lu);
+        else ops.factor((Cf)ghinv, lu);
         T hinv = one / hs;
 
 #pragma unroll
@@ -375,12 +459,17 @@ struct Lane {
                         ytmp[s] = sgb_fma(av, K[j][s], ytmp[s]);
                     }
                 }
-                eval_point(ytmp, at);
-                ops.fun(k, src, at, fcn);
+                if constexpr (kMixed) {
+                    rhs_df(ytmp);
+                } else {
+                    eval_point(ytmp, at);
+                    ops.fun(k, src, at, fcn);
+                }
             }
             for (int s = 0; s < N; ++s) {
                 if (s >= (int)nn) break;
-                K[st][s] = (T)fcn[s];
+                if constexpr (kMixed) K[st][s] = df_to(Df{fhi[s], flo[s]});
+                else K[st][s] = (T)fcn[s];
             }
 #pragma unroll
             for (int j = 0; j < st; ++j) {
@@ -474,6 +563,10 @@ struct GenOps {
     template <class T> __device__ __forceinline__ void neg_jac(const T *k, const T *y, T *a) const { G::neg_jac(k, y, a); }
     template <class T> __device__ __forceinline__ void factor(T ghinv, T *a) const { G::factor(ghinv, a); }
     template <class T> __device__ __forceinline__ void solve(const T *a, T *x) const { G::solve(a, x); }
+    __device__ __forceinline__ void fun_df(const float *khi, const float *klo, const float *shi, const float *slo, const float *yhi,
+                                           const float *ylo, float *fhi, float *flo) const {
+        G::fun_df(khi, klo, shi, slo, yhi, ylo, fhi, flo);
+    }
     __device__ __forceinline__ void save_jac(const float *a, float *js) const { G::save_jac(a, js); }
     __device__ __forceinline__ void residual(const float *js, double ghinv, const double *b, const double *x, double *r) const {
         G::residual(js, ghinv, b, x, r);

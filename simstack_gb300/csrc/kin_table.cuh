@@ -10,7 +10,11 @@
 
 namespace sgb {
 
-constexpr uint32_t kTableBytes = (uint32_t)((sizeof(KinMech) + 15) / 16 * 16);
+// Staged image: the KinMech record, then a bitmask of the compact slots that
+// belong to the Jacobian's own pattern (before fill-in), used by the mixed
+// path's residual.
+constexpr uint32_t kJacMaskOffset = (uint32_t)((sizeof(KinMech) + 15) / 16 * 16);
+constexpr uint32_t kTableBytes = kJacMaskOffset + KIN_MAX_NNZ / 8;
 
 struct TableOps {
     static constexpr int N = KIN_MAX_SPECIES, R = KIN_MAX_REACTIONS, NNZ = KIN_MAX_NNZ, NJ = KIN_MAX_NNZ;
@@ -102,22 +106,53 @@ struct TableOps {
         }
     }
 
+    // Double-float RHS in the generated code's order (kin_codegen.cpp, fun_df).
+    __device__ __forceinline__ void fun_df(const float *khi, const float *klo, const float *shi, const float *slo, const float *yhi,
+                                           const float *ylo, float *fhi, float *flo) const {
+        const uint32_t ns = m->species_count, nr = m->reaction_count;
+        for (uint32_t s = 0; s < ns; ++s) {
+            fhi[s] = shi[s];
+            flo[s] = slo[s];
+        }
+        for (uint32_t r = 0; r < nr; ++r) {
+            const KinReaction &rx = m->reactions[r];
+            Df rate{khi[r], klo[r]};
+            for (uint32_t p = 0; p < rx.reactant_count; ++p) rate = df_mul(rate, Df{yhi[rx.reactant[p]], ylo[rx.reactant[p]]});
+            for (uint32_t e = 0; e < rx.net_count; ++e) {
+                const uint32_t s = rx.net_species[e];
+                const int c = rx.net_coef[e];
+                Df term = c == 1 ? rate
+                          : (c == -1 || c == 2 || c == -2 || c == 4 || c == -4) ? df_scale(rate, (float)c)
+                                                                                 : df_mul(rate, Df{(float)c, 0.0f});
+                const Df acc = df_add(Df{fhi[s], flo[s]}, term);
+                fhi[s] = acc.hi;
+                flo[s] = acc.lo;
+            }
+        }
+    }
+
+    __device__ __forceinline__ bool in_jac(uint32_t slot) const {
+        const uint8_t *mask = (const uint8_t *)m + kJacMaskOffset;
+        return (mask[slot >> 3] >> (slot & 7)) & 1u;
+    }
+
     // Mixed path: keep all of -J (fill-in slots are zero) before the factorisation.
     __device__ __forceinline__ void save_jac(const float *a, float *js) const {
         const uint32_t nz = m->nnz;
         for (uint32_t i = 0; i < nz; ++i) js[i] = a[i];
     }
 
-    // r = b - ghinv x - (-J) x in FP64.
+    // r = b - ghinv x - (-J) x in FP64, over each row's Jacobian-pattern
+    // entries in ascending column order (the generated code's order).
     __device__ __forceinline__ void residual(const float *js, double ghinv, const double *b, const double *x, double *r) const {
         const uint32_t ns = m->species_count;
         for (uint32_t i = 0; i < ns; ++i) {
             double acc = sgb_fma(-ghinv, x[i], b[i]);
-            acc = sgb_fma(-(double)js[m->diag[i]], x[i], acc);
             for (uint32_t e = m->lower_begin[i]; e < m->lower_begin[i + 1]; ++e)
-                acc = sgb_fma(-(double)js[m->lower[e].index], x[m->lower[e].col], acc);
-            for (uint32_t e = m->upper_begin[i]; e < m->upper_begin[i + 1]; ++e)
-                acc = sgb_fma(-(double)js[m->upper[e].index], x[m->upper[e].col], acc);
+                if (in_jac(m->lower[e].index)) acc = sgb_fma(-cvt_f2d(js[m->lower[e].index]), x[m->lower[e].col], acc);
+            acc = sgb_fma(-cvt_f2d(js[m->diag[i]]), x[i], acc);
+            for (uint32_t e = m->upper_begin[i + 1]; e-- > m->upper_begin[i];)
+                if (in_jac(m->upper[e].index)) acc = sgb_fma(-cvt_f2d(js[m->upper[e].index]), x[m->upper[e].col], acc);
             r[i] = acc;
         }
     }
