@@ -188,8 +188,9 @@ SGB_API int32_t gpu_kin_set_mode(uint32_t mode);
 SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_ms);
 
 /* Launch tuning. kind: 0 static one-cell-per-thread, 1 persistent queue.
- * block = threads per CTA (multiple of 32), chunk = cells claimed per queue
- * pop, variant = compiled register-budget variant (0: 255 regs, 1: 128, 2: 96).
+ * block = threads per CTA (multiple of 32, <= 128), chunk = resident CTAs per
+ * SM for the queue kernel (0: as many as fit), variant = compiled
+ * register-budget variant (0: up to 255 registers, 1: 128).
  * gpu_kin_autotune times candidates on the given launch (which it advances
  * repeatedly on a scratch copy it restores) and keeps the fastest. */
 typedef struct GpuKinTuning {

@@ -827,7 +827,9 @@ static void advance_range(const Mechanism *m, const Method *me, const Control *c
 // Model of this module's MIXED-precision attempt (not a reference algorithm:
 // the reference has no mixed path), in the GPU kernel's operation order so
 // the tests can compare the GPU's mixed kernel with it bit for bit:
-//   RHS      double-float (hi + lo FP32 pairs) at the FP64 stage point
+//   RHS      f(y) once per step in double-float (hi + lo FP32 pairs); at the
+//            other stage points Y = y + d, f(y) + df with df in FP32 from the
+//            exact increment expansion (eval_fun_delta32)
 //   -J, LU   FP32 at the FP32 rounding of the point
 //   solve    FP32 LU solve, then `sweeps` refinement sweeps with the FP64
 //            residual r = b - ghinv x - (-J) x over the Jacobian pattern
@@ -903,8 +905,29 @@ static void residual64(const Mechanism &m, const float *js, double ghinv, const 
     }
 }
 
+// Stage RHS in increment form: f(y + d) = f(y) + df with df evaluated in FP32
+// from the exact expansion prod(y_q + d_q) - prod(y_q) =
+// sum_p (prod_{q<p} y_q) d_p (prod_{q>p} (y_q + d_q)), per reaction.
+static void eval_fun_delta32(const Mechanism &m, const float *k, const float *y, const float *d, float *df) {
+    for (u32 s = 0; s < m.n(); ++s) df[s] = 0.0f;
+    for (u32 r = 0; r < m.R(); ++r) {
+        const Reaction &rx = m.reactions[r];
+        float rate = 0.0f;
+        for (u32 p = 0; p < rx.reactant_count; ++p) {
+            float term = k[r] * d[rx.reactant[p]];   // k first: keeps products of large densities in FP32 range
+            for (u32 q = 0; q < p; ++q) term = term * y[rx.reactant[q]];
+            for (u32 q = p + 1; q < rx.reactant_count; ++q) term = term * (y[rx.reactant[q]] + d[rx.reactant[q]]);
+            rate = rate + term;
+        }
+        for (u32 e = 0; e < rx.net_count; ++e) df[rx.net_species[e]] = std::fma((float)rx.net_coef[e], rate, df[rx.net_species[e]]);
+    }
+}
+
 static void integrate_mixed(const Mechanism &m, const Method &me, const Control &ctl, u32 sweeps, double *y, double &t,
                             double t_end, double &h, Stats<double> &st, MixedWork &w) {
+    std::vector<double> f0(m.n());
+    std::vector<float> d32(m.n()), df32(m.n());
+    std::vector<double> fcur(m.n());
     const u32 n = m.n();
     const double zero = 0.0, one = 1.0, h_min = ctl.h_min, rtol = ctl.rtol, atol = ctl.atol;
     const double inv_n = 1.0 / (double)n;
@@ -932,6 +955,8 @@ static void integrate_mixed(const Mechanism &m, const Method &me, const Control 
         double hs = last ? remaining : vmin(h_wanted, h_cap);
 
         rhs(y);
+        for (u32 s = 0; s < n; ++s) f0[s] = df_to(w.fd[s]);
+        for (u32 s = 0; s < n; ++s) fcur[s] = f0[s];
         for (u32 s = 0; s < n; ++s) yhi[s] = w.yd[s].hi;
         eval_neg_jac(m, w.k32.data(), yhi.data(), a);
         for (u32 i = 0; i < m.nnz; ++i) js[i] = a[i];
@@ -941,16 +966,27 @@ static void integrate_mixed(const Mechanism &m, const Method &me, const Control 
 
         for (u32 stg = 0; stg < me.stages; ++stg) {
             u32 packed = stg * (stg - 1) / 2;
+            // stage RHS: f(y) from the step start when the stage point is y itself
+            // (no nonzero a coefficient, e.g. Rodas3 stage 2), else f(y) + df with
+            // df the FP32 increment form at d = Y - y
+            bool moved = false;
             if (stg > 0 && me.new_f[stg]) {
                 for (u32 s = 0; s < n; ++s) ytmp[s] = y[s];
                 for (u32 j = 0; j < stg; ++j) {
                     double av = me.a[packed + j];
                     if (av == 0.0) continue;
+                    moved = true;
                     for (u32 s = 0; s < n; ++s) ytmp[s] = std::fma(av, K[j][s], ytmp[s]);
                 }
-                rhs(ytmp);
+                if (moved) {
+                    for (u32 s = 0; s < n; ++s) d32[s] = (float)(ytmp[s] - y[s]);
+                    eval_fun_delta32(m, w.k32.data(), yhi.data(), d32.data(), df32.data());
+                    for (u32 s = 0; s < n; ++s) fcur[s] = f0[s] + (double)df32[s];
+                } else {
+                    for (u32 s = 0; s < n; ++s) fcur[s] = f0[s];
+                }
             }
-            for (u32 s = 0; s < n; ++s) K[stg][s] = df_to(w.fd[s]);
+            for (u32 s = 0; s < n; ++s) K[stg][s] = fcur[s];
             for (u32 j = 0; j < stg; ++j) {
                 double c = me.c[packed + j];
                 if (c == 0.0) continue;

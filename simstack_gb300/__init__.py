@@ -431,8 +431,8 @@ class Module:
             check(lib().gpu_kin_advance(C.byref(L), C.byref(ms)), "gpu_kin_advance")
         return ms.value
 
-    def set_tuning(self, kind: int = 1, block: int = 128, variant: int = 0) -> None:
-        t = GpuKinTuning(kind, block, 1, variant, 0.0)
+    def set_tuning(self, kind: int = 1, block: int = 128, variant: int = 0, ctas_per_sm: int = 0) -> None:
+        t = GpuKinTuning(kind, block, ctas_per_sm, variant, 0.0)
         check(lib().gpu_kin_set_tuning(C.byref(t)), "gpu_kin_set_tuning")
 
     def tuning(self, precision: int = 0) -> GpuKinTuning:

@@ -33,6 +33,8 @@ CXX = os.environ.get("CXX", "g++")
 
 NV_FLAGS = ["-std=c++17", "-O3", ARCH, "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC,-ffp-contract=off",
             "-Xptxas", "-v", f"-I{GEN}", f"-I{CSRC}"]
+# Extra preprocessor definitions for build-time variants (e.g. SGB_NOINLINE_OPS).
+NV_FLAGS += [f"-D{d}" for d in os.environ.get("SGB_DEFINES", "").split() if d]
 CXX_FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-fno-fast-math", "-Wall", "-Wno-unused-function"]
 
 

@@ -57,7 +57,7 @@ struct Module {
 };
 Module g;
 
-const GpuKinTuning kDefaultTuning = {1u, 128u, 1u, 0u, 0.0f};
+const GpuKinTuning kDefaultTuning = {1u, 128u, 0u, 0u, 0.0f};
 
 bool is_rodas3(const KinMethod *m) {
     KinMethod r = method_coefficients(2);
@@ -116,6 +116,7 @@ cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &
         cudaError_t e = occupancy(prec, t, &per_sm);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
+        if (t.chunk > 0 && (int)t.chunk < per_sm) per_sm = (int)t.chunk;   // chunk: CTAs per SM (0 = as many as fit)
         uint32_t resident = (uint32_t)per_sm * (uint32_t)g.sms;
         uint32_t needed = (A.lanes + t.block - 1) / t.block;
         s.grid = resident < needed ? resident : needed;
@@ -429,7 +430,7 @@ SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_
 }
 
 SGB_API int32_t gpu_kin_set_tuning(const GpuKinTuning *t) {
-    if (!t || t->kind > 1 || t->block == 0 || t->block > 128 || (t->block & 31) || t->variant > 1)
+    if (!t || t->kind > 1 || t->block == 0 || t->block > 128 || (t->block & 31) || t->variant > 1 || t->chunk > 64)
         return (int32_t)cudaErrorInvalidValue;
     for (int p = 0; p < 3; ++p) g.tuning[p] = *t;
     return 0;
@@ -465,12 +466,17 @@ SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuK
         }
     };
     copy_all(true);
-    const uint32_t blocks[3] = {32, 64, 128};
+    // candidates: block size x register budget x resident CTAs per SM (queue kernel)
+    struct Cand { uint32_t block, variant, ctas; };
+    const Cand cands[] = {{32, 0, 0}, {64, 0, 0}, {128, 0, 0}, {64, 1, 0}, {128, 1, 0},
+                          {128, 0, 1}, {64, 0, 2}, {64, 0, 3}, {128, 1, 2}, {128, 1, 3}};
     GpuKinTuning winner = g.tuning[launch->precision];
     winner.ms = 1e30f;
-    for (uint32_t v = 0; v < 2 && e == cudaSuccess; ++v)
-        for (uint32_t b : blocks) {
-            GpuKinTuning t = {kind, b, 1u, v, 0.0f};
+    for (const Cand &c : cands) {
+        if (e != cudaSuccess) break;
+        if (kind == 0 && c.ctas != 0) continue;
+        {
+            GpuKinTuning t = {kind, c.block, c.ctas, c.variant, 0.0f};
             float ms = 0.0f;
             e = advance_sync(launch, t, &ms);
             copy_all(false);
@@ -480,6 +486,7 @@ SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuK
                 winner.ms = ms;
             }
         }
+    }
     cudaStreamSynchronize(g.stream);
     cudaFree(save);
     if (e != cudaSuccess) return (int32_t)e;

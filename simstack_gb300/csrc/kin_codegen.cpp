@@ -82,6 +82,24 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
     for (uint32_t s = 0; s < n; ++s) fprintf(f, "        fhi[%u] = acc[%u].hi; flo[%u] = acc[%u].lo;\n", s, s, s, s);
     fprintf(f, "    }\n\n");
 
+    // mixed path: FP32 RHS increment f(y + d) - f(y) from the exact expansion
+    // prod(y_q + d_q) - prod(y_q) = sum_p k d_p prod_{q<p} y_q prod_{q>p} (y_q + d_q)
+    fprintf(f, "    static __device__ __forceinline__ void fun_delta(const float *__restrict__ k, const float *__restrict__ y, const float *__restrict__ d, float *__restrict__ df) {\n");
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        df[%u] = 0.0f;\n", s);
+    for (uint32_t r = 0; r < R; ++r) {
+        const Reaction &rx = m.reactions[r];
+        fprintf(f, "        { float rate = 0.0f;\n");
+        for (size_t p = 0; p < rx.reactants.size(); ++p) {
+            fprintf(f, "          { float term = k[%u] * d[%u];", r, rx.reactants[p]);
+            for (size_t q = 0; q < p; ++q) fprintf(f, " term = term * y[%u];", rx.reactants[q]);
+            for (size_t q = p + 1; q < rx.reactants.size(); ++q) fprintf(f, " term = term * (y[%u] + d[%u]);", rx.reactants[q], rx.reactants[q]);
+            fprintf(f, " rate = rate + term; }\n");
+        }
+        for (auto &e : rx.net) fprintf(f, "          df[%u] = fmaf(%d.0f, rate, df[%u]);\n", e.first, e.second, e.first);
+        fprintf(f, "        }\n");
+    }
+    fprintf(f, "    }\n\n");
+
     // -J into the compact LU storage
     fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void neg_jac(const T *__restrict__ k, const T *__restrict__ y, T *__restrict__ a) {\n");
     std::vector<uint8_t> written(S.nnz, 0);
@@ -137,16 +155,16 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
     }
     fprintf(f, "    }\n\n");
 
-    // mixed path: keep -J's pattern entries (FP32) before the factorisation
-    fprintf(f, "    static __device__ __forceinline__ void save_jac(const float *__restrict__ a, float *__restrict__ js) {\n");
-    for (size_t q = 0; q < jslots.size(); ++q) fprintf(f, "        js[%zu] = a[%u];\n", q, jslots[q]);
+    // mixed path: keep -J's pattern entries, widened to FP64 once per step, before the factorisation
+    fprintf(f, "    static __device__ __forceinline__ void save_jac(const float *__restrict__ a, double *__restrict__ js) {\n");
+    for (size_t q = 0; q < jslots.size(); ++q) fprintf(f, "        js[%zu] = (double)a[%u];\n", q, jslots[q]);
     fprintf(f, "    }\n\n");
     // r = b - W x = b - ghinv x - (-J) x, in FP64 (the -J entries are exact FP32 values)
-    fprintf(f, "    static __device__ __forceinline__ void residual(const float *__restrict__ js, double ghinv, const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r) {\n");
+    fprintf(f, "    static __device__ __forceinline__ void residual(const double *__restrict__ js, double ghinv, const double *__restrict__ b, const double *__restrict__ x, double *__restrict__ r) {\n");
     for (uint32_t i = 0; i < n; ++i) {
         fprintf(f, "        { double acc = sgb_fma(-ghinv, x[%u], b[%u]);\n", i, i);
         for (size_t q = 0; q < jslots.size(); ++q)
-            if (jrow[q] == i) fprintf(f, "          acc = sgb_fma(-cvt_f2d(js[%zu]), x[%u], acc);\n", q, jcol[q]);
+            if (jrow[q] == i) fprintf(f, "          acc = sgb_fma(-js[%zu], x[%u], acc);\n", q, jcol[q]);
         fprintf(f, "          r[%u] = acc; }\n", i);
     }
     fprintf(f, "    }\n");

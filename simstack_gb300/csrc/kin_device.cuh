@@ -64,45 +64,16 @@ __device__ __forceinline__ float sgb_first_neg(float d) {
     return __uint_as_float((b << 1) == 0 ? 0u : (b ^ 0x80000000u));
 }
 
-// Exact FP32 <-> FP64 conversions on the integer pipe. On GB300 the
-// hardware conversion instructions issue at the FP64 rate (measured: ~2 per
-// clock per SM), so the mixed path would spend its FP64 budget converting;
-// these produce the same bits as cvt.f64.f32 / cvt.rn.f32.f64 for normal
-// values and zeros and defer to the hardware instruction for subnormals,
-// infinities and NaNs.
-__device__ __forceinline__ double cvt_f2d(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned e = (u >> 23) & 0xFFu;
-    if (e - 1u < 254u) {
-        const unsigned hi = (u & 0x80000000u) | ((e + 896u) << 20) | ((u >> 3) & 0x000FFFFFu);
-        return __hiloint2double((int)hi, (int)(u << 29));
-    }
-    if ((u << 1) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    return (double)f;
-}
-__device__ __forceinline__ float cvt_d2f(double d) {
-    const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
-    const unsigned e = (hi >> 20) & 0x7FFu;
-    if (e - 897u < 254u) {   // result is a normal float (biased exponent 1..254) before rounding
-        unsigned r = ((e - 896u) << 23) | ((hi & 0x000FFFFFu) << 3) | (lo >> 29);
-        const unsigned rest = lo & 0x1FFFFFFFu, half = 0x10000000u;
-        r += (unsigned)((rest > half) | ((rest == half) & (r & 1u)));   // round to nearest even; a carry moves the exponent
-        return __uint_as_float((hi & 0x80000000u) | r);
-    }
-    if (((hi << 1) | lo) == 0u) return __uint_as_float(hi & 0x80000000u);
-    return __double2float_rn(d);
-}
-
 // Double-float arithmetic: a value is hi + lo, two FP32 numbers (~48-bit
 // significand). The mixed path evaluates the RHS this way on the FP32 pipe.
 struct Df {
     float hi, lo;
 };
 __device__ __forceinline__ Df df_from(double d) {
-    const float h = cvt_d2f(d);
-    return Df{h, cvt_d2f(d - cvt_f2d(h))};   // d - h is exact in FP64
+    const float h = (float)d;
+    return Df{h, (float)(d - (double)h)};   // d - h is exact in FP64
 }
-__device__ __forceinline__ double df_to(Df a) { return cvt_f2d(a.hi) + cvt_f2d(a.lo); }
+__device__ __forceinline__ double df_to(Df a) { return (double)a.hi + (double)a.lo; }
 __device__ __forceinline__ Df df_mul(Df a, Df b) {
     const float p = a.hi * b.hi;
     float e = fmaf(a.hi, b.hi, -p);
@@ -230,7 +201,9 @@ struct Lane {
     float yhi[kMixed ? N : 1], ylo[kMixed ? N : 1], fhi[kMixed ? N : 1], flo[kMixed ? N : 1];   // mixed: double-float point, RHS
     T ytmp[N];
     T K[S][N];
-    float js[kMixed ? Ops::NJ : 1];            // mixed: -J pattern entries before the factorisation
+    double js[kMixed ? Ops::NJ : 1];           // mixed: -J pattern entries (FP64) before the factorisation
+    double f0[kMixed ? N : 1];                 // mixed: f(y) at the step start
+    float d32[kMixed ? N : 1], df32[kMixed ? N : 1];   // mixed: stage increment and its RHS increment
     double rb[kMixed ? N : 1];                 // mixed: stage right-hand side b
     double rr[kMixed ? N : 1];                 // mixed: residual
     float x32[kMixed ? N : 1];
@@ -390,23 +363,23 @@ struct Lane {
         const uint32_t nn = n();
         for (int s = 0; s < N; ++s) {
             if (s >= (int)nn) break;
-            x32[s] = cvt_d2f(rb[s]);
+            x32[s] = (float)rb[s];
         }
         ops.solve(lu, x32);
         for (int s = 0; s < N; ++s) {
             if (s >= (int)nn) break;
-            x[s] = cvt_f2d(x32[s]);
+            x[s] = (double)x32[s];
         }
         for (uint32_t sw = 0; sw < A.ir_sweeps; ++sw) {
             ops.residual(js, ghinv, rb, x, rr);
             for (int s = 0; s < N; ++s) {
                 if (s >= (int)nn) break;
-                x32[s] = cvt_d2f(rr[s]);
+                x32[s] = (float)rr[s];
             }
             ops.solve(lu, x32);
             for (int s = 0; s < N; ++s) {
                 if (s >= (int)nn) break;
-                x[s] = x[s] + cvt_f2d(x32[s]);
+                x[s] = x[s] + (double)x32[s];
             }
         }
     }
@@ -428,6 +401,10 @@ struct Lane {
         const Cf *at = nullptr;
         if constexpr (kMixed) {
             rhs_df(y);
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                f0[s] = df_to(Df{fhi[s], flo[s]});
+            }
             ops.neg_jac(khi, yhi, lu);   // FP32 Jacobian at the FP32 rounding of y
             ops.save_jac(lu, js);
         } else {
@@ -436,15 +413,20 @@ struct Lane {
             ops.neg_jac(k, at, lu);
         }
         T ghinv = one / (hs * (T)M::gamma0(A));
-        if constexpr (kMixed) ops.factor(cvt_d2f(ghinv), lu);
+        if constexpr (kMixed) ops.factor((float)ghinv, lu);
         else ops.factor((Cf)ghinv, lu);
         T hinv = one / hs;
 
-#pragma unroll
+        bool fcn_at_y = true;   // fcn (plain paths) holds f at the step-start point
+        bool last_moved = false;   // mixed: the last stage RHS was f(y) + df32 (else f(y))
+#pragma unroll(kMixed ? 1 : S)
         for (int st = 0; st < S; ++st) {
             if (st >= M::stages(A)) break;
             const int packed = st * (st - 1) / 2;
             if (st > 0 && M::new_f(A, st)) {
+                // stage point Y = y + sum_j a_j K_j; when no a_j is nonzero Y is y
+                // itself (Rodas3 stage 2) and f(Y) = f(y) is reused, bit for bit
+                bool moved = false;
                 for (int s = 0; s < N; ++s) {
                     if (s >= (int)nn) break;
                     ytmp[s] = y[s];
@@ -453,6 +435,7 @@ struct Lane {
                 for (int j = 0; j < st; ++j) {
                     double a = M::a(A, packed + j);
                     if (a == 0.0) continue;
+                    moved = true;
                     T av = (T)a;
                     for (int s = 0; s < N; ++s) {
                         if (s >= (int)nn) break;
@@ -460,16 +443,30 @@ struct Lane {
                     }
                 }
                 if constexpr (kMixed) {
-                    rhs_df(ytmp);
-                } else {
+                    if (moved) {
+                        for (int s = 0; s < N; ++s) {
+                            if (s >= (int)nn) break;
+                            d32[s] = (float)(ytmp[s] - y[s]);
+                        }
+                        ops.fun_delta(khi, yhi, d32, df32);
+                    }
+                    last_moved = moved;
+                } else if (moved || !fcn_at_y) {
                     eval_point(ytmp, at);
                     ops.fun(k, src, at, fcn);
+                    fcn_at_y = !moved;
                 }
-            }
-            for (int s = 0; s < N; ++s) {
-                if (s >= (int)nn) break;
-                if constexpr (kMixed) K[st][s] = df_to(Df{fhi[s], flo[s]});
-                else K[st][s] = (T)fcn[s];
+                for (int s = 0; s < N; ++s) {
+                    if (s >= (int)nn) break;
+                    if constexpr (kMixed) K[st][s] = moved ? f0[s] + (double)df32[s] : f0[s];
+                    else K[st][s] = (T)fcn[s];
+                }
+            } else {   // no new evaluation: the last stage RHS again
+                for (int s = 0; s < N; ++s) {
+                    if (s >= (int)nn) break;
+                    if constexpr (kMixed) K[st][s] = last_moved ? f0[s] + (double)df32[s] : f0[s];
+                    else K[st][s] = (T)fcn[s];
+                }
             }
 #pragma unroll
             for (int j = 0; j < st; ++j) {
@@ -553,22 +550,33 @@ struct Lane {
 // ---------------------------------------------------------------------------
 // Generated straight-line ops (kin_codegen.cpp) as an Ops object.
 
+// SGB_OPS_QUALIFIER: __forceinline__ (default) inlines every op at every call
+// site; building with -DSGB_NOINLINE_OPS keeps one copy of each op's body
+// (smaller code, more calls) -- a build-time variant for the instruction-cache
+// experiments.
+#ifdef SGB_NOINLINE_OPS
+#define SGB_OPS_QUALIFIER __noinline__
+#else
+#define SGB_OPS_QUALIFIER __forceinline__
+#endif
+
 template <class G>
 struct GenOps {
     static constexpr int N = G::N, R = G::R, NNZ = G::NNZ, NJ = G::NJ;
     __device__ __forceinline__ uint32_t n() const { return (uint32_t)N; }
     __device__ __forceinline__ uint32_t r() const { return (uint32_t)R; }
     __device__ __forceinline__ bool init(const DevArgs &, unsigned char *) { return true; }
-    template <class T> __device__ __forceinline__ void fun(const T *k, const T *src, const T *y, T *f) const { G::fun(k, src, y, f); }
-    template <class T> __device__ __forceinline__ void neg_jac(const T *k, const T *y, T *a) const { G::neg_jac(k, y, a); }
-    template <class T> __device__ __forceinline__ void factor(T ghinv, T *a) const { G::factor(ghinv, a); }
-    template <class T> __device__ __forceinline__ void solve(const T *a, T *x) const { G::solve(a, x); }
-    __device__ __forceinline__ void fun_df(const float *khi, const float *klo, const float *shi, const float *slo, const float *yhi,
-                                           const float *ylo, float *fhi, float *flo) const {
+    template <class T> __device__ SGB_OPS_QUALIFIER void fun(const T *k, const T *src, const T *y, T *f) const { G::fun(k, src, y, f); }
+    template <class T> __device__ SGB_OPS_QUALIFIER void neg_jac(const T *k, const T *y, T *a) const { G::neg_jac(k, y, a); }
+    template <class T> __device__ SGB_OPS_QUALIFIER void factor(T ghinv, T *a) const { G::factor(ghinv, a); }
+    template <class T> __device__ SGB_OPS_QUALIFIER void solve(const T *a, T *x) const { G::solve(a, x); }
+    __device__ SGB_OPS_QUALIFIER void fun_df(const float *khi, const float *klo, const float *shi, const float *slo, const float *yhi,
+                                             const float *ylo, float *fhi, float *flo) const {
         G::fun_df(khi, klo, shi, slo, yhi, ylo, fhi, flo);
     }
-    __device__ __forceinline__ void save_jac(const float *a, float *js) const { G::save_jac(a, js); }
-    __device__ __forceinline__ void residual(const float *js, double ghinv, const double *b, const double *x, double *r) const {
+    __device__ SGB_OPS_QUALIFIER void fun_delta(const float *k, const float *y, const float *d, float *df) const { G::fun_delta(k, y, d, df); }
+    __device__ SGB_OPS_QUALIFIER void save_jac(const float *a, double *js) const { G::save_jac(a, js); }
+    __device__ SGB_OPS_QUALIFIER void residual(const double *js, double ghinv, const double *b, const double *x, double *r) const {
         G::residual(js, ghinv, b, x, r);
     }
 };

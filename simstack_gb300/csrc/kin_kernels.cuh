@@ -23,6 +23,12 @@ template <int V> struct Budget;
 template <> struct Budget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
 template <> struct Budget<1> { static constexpr int kThreads = 128, kMinBlocks = 4; };
 
+// Both kernels keep every lane of a warp in the loop until the whole warp is
+// out of work, and vote (__any_sync) once per iteration: the vote is a
+// reconvergence point, so all lanes that need a step attempt run it together
+// and the attempt's straight-line code issues once per warp, not once per
+// diverged group of lanes. Blocks are whole warps.
+
 template <class Ops, class M, int PREC, int V>
 __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_static_kernel(const __grid_constant__ DevArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
@@ -32,10 +38,20 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
         return;
     }
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= A.lanes) return;
-    L.load(A, i);
-    while (L.settle(A, i)) L.attempt(A);
-    L.store(A, i);
+    bool have = i < A.lanes;
+    if (have) L.load(A, i);
+    for (;;) {
+        bool need = false;
+        if (have) {
+            need = L.settle(A, i);
+            if (!need) {
+                L.store(A, i);
+                have = false;
+            }
+        }
+        if (!__any_sync(0xffffffffu, need)) break;
+        if (need) L.attempt(A);
+    }
 }
 
 template <class Ops, class M, int PREC, int V>
@@ -46,14 +62,17 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
         if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
         return;
     }
-    bool have = false;
+    bool have = false, exhausted = false;
     uint32_t cell = 0;
     for (;;) {
         bool need = false;
-        for (;;) {
+        while (!exhausted) {   // this lane: finish, store and replace cells until one needs an attempt
             if (!have) {
                 cell = atomicAdd(A.cursor, 1u);
-                if (cell >= A.lanes) break;
+                if (cell >= A.lanes) {
+                    exhausted = true;
+                    break;
+                }
                 L.load(A, cell);
                 have = true;
             }
@@ -64,8 +83,8 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
             L.store(A, cell);
             have = false;
         }
-        if (!need) break;
-        L.attempt(A);
+        if (!__any_sync(0xffffffffu, need)) break;
+        if (need) L.attempt(A);
     }
 }
 
@@ -89,6 +108,10 @@ void (*kernel_for(uint32_t kind, uint32_t variant))(DevArgs) {
 template <class Ops, class M, int PREC, int kVariants = 2>
 cudaError_t launch_one(const Shape &s, const DevArgs &A, cudaStream_t stream) {
     void (*fn)(DevArgs) = kernel_for<Ops, M, PREC, kVariants>(s.kind, s.variant);
+    if (s.smem == 0) {   // no shared memory: give the unified L1/shared array to L1 (local-memory spills live there)
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
+        if (e != cudaSuccess) return e;
+    }
     if (s.smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
         if (e != cudaSuccess) return e;

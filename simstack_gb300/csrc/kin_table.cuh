@@ -136,23 +136,40 @@ struct TableOps {
         return (mask[slot >> 3] >> (slot & 7)) & 1u;
     }
 
-    // Mixed path: keep all of -J (fill-in slots are zero) before the factorisation.
-    __device__ __forceinline__ void save_jac(const float *a, float *js) const {
+    // FP32 RHS increment at y + d (kin_codegen.cpp, fun_delta).
+    __device__ __forceinline__ void fun_delta(const float *k, const float *y, const float *d, float *df) const {
+        const uint32_t ns = m->species_count, nr = m->reaction_count;
+        for (uint32_t s = 0; s < ns; ++s) df[s] = 0.0f;
+        for (uint32_t r = 0; r < nr; ++r) {
+            const KinReaction &rx = m->reactions[r];
+            float rate = 0.0f;
+            for (uint32_t p = 0; p < rx.reactant_count; ++p) {
+                float term = k[r] * d[rx.reactant[p]];
+                for (uint32_t q = 0; q < p; ++q) term = term * y[rx.reactant[q]];
+                for (uint32_t q = p + 1; q < rx.reactant_count; ++q) term = term * (y[rx.reactant[q]] + d[rx.reactant[q]]);
+                rate = rate + term;
+            }
+            for (uint32_t e = 0; e < rx.net_count; ++e) df[rx.net_species[e]] = fmaf((float)rx.net_coef[e], rate, df[rx.net_species[e]]);
+        }
+    }
+
+    // Mixed path: keep all of -J (fill-in slots are zero), widened to FP64, before the factorisation.
+    __device__ __forceinline__ void save_jac(const float *a, double *js) const {
         const uint32_t nz = m->nnz;
-        for (uint32_t i = 0; i < nz; ++i) js[i] = a[i];
+        for (uint32_t i = 0; i < nz; ++i) js[i] = (double)a[i];
     }
 
     // r = b - ghinv x - (-J) x in FP64, over each row's Jacobian-pattern
     // entries in ascending column order (the generated code's order).
-    __device__ __forceinline__ void residual(const float *js, double ghinv, const double *b, const double *x, double *r) const {
+    __device__ __forceinline__ void residual(const double *js, double ghinv, const double *b, const double *x, double *r) const {
         const uint32_t ns = m->species_count;
         for (uint32_t i = 0; i < ns; ++i) {
             double acc = sgb_fma(-ghinv, x[i], b[i]);
             for (uint32_t e = m->lower_begin[i]; e < m->lower_begin[i + 1]; ++e)
-                if (in_jac(m->lower[e].index)) acc = sgb_fma(-cvt_f2d(js[m->lower[e].index]), x[m->lower[e].col], acc);
-            acc = sgb_fma(-cvt_f2d(js[m->diag[i]]), x[i], acc);
+                if (in_jac(m->lower[e].index)) acc = sgb_fma(-js[m->lower[e].index], x[m->lower[e].col], acc);
+            acc = sgb_fma(-js[m->diag[i]], x[i], acc);
             for (uint32_t e = m->upper_begin[i + 1]; e-- > m->upper_begin[i];)
-                if (in_jac(m->upper[e].index)) acc = sgb_fma(-cvt_f2d(js[m->upper[e].index]), x[m->upper[e].col], acc);
+                if (in_jac(m->upper[e].index)) acc = sgb_fma(-js[m->upper[e].index], x[m->upper[e].col], acc);
             r[i] = acc;
         }
     }
