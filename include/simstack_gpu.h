@@ -219,6 +219,27 @@ SGB_API int32_t gpu_copy_on_device(void *dst_device, const void *src_device, uin
 /* The module's stream (a cudaStream_t), for callers ordering their own work against it. */
 SGB_API void *gpu_stream(void);
 
+/* No counterpart in the reference. The persistent work-queue advance for
+ * callers that cannot allocate device memory: a caller whose device memory is
+ * all owned by its own arena (SimStack's platform hands the simulation one
+ * fixed block), a caller recording into a CUDA graph (allocations cannot be
+ * captured) or a real-time loop that may not take cudaMalloc's device-wide
+ * synchronisation. It needs no gpu_init and calls no cudaMalloc, cudaFree or
+ * other allocating routine. Its scratch -- queue cursor, error flag and, for
+ * mechanisms without generated code, the staged tables -- lives in a static
+ * device array of 32 KiB that every GPU holds from library load to process
+ * exit; a call whose scratch would exceed it returns
+ * cudaErrorMemoryAllocation. mech / method / control are as for
+ * gpu_kin_set_mech, the launch as for gpu_kin_advance (device pointers);
+ * the work is enqueued on `stream` (a cudaStream_t, 0 = default stream) and,
+ * if `wait` is nonzero, waited for and its error flag checked. The first call
+ * on a device looks up the array's device address with that device current:
+ * make it before any stream capture. Every call shares the array and clears
+ * what must start at zero; calls that overlap on the GPU (other streams,
+ * other host threads) race on it. */
+SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *method, const KinControl *control,
+                                        const GpuKinLaunch *launch, void *stream, int32_t wait);
+
 /* ---------------------------------------------------------------------------
  * Host-side mechanism compiler: src/sim/kinetics/kin_build.cpp:199-365 and
  * air_mech.cpp:30-108, 205-276. Builds the reference-layout KinMech (same

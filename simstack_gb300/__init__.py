@@ -140,6 +140,8 @@ def lib() -> C.CDLL:
             "gpu_probe_throughput": (i32, [u32, C.POINTER(d)]),
             "gpu_stream": (vp, []),
             "gpu_copy_on_device": (i32, [vp, vp, u64]),
+            "gpu_kin_advance_noalloc": (i32, [C.POINTER(KinMech), C.POINTER(KinMethod), C.POINTER(KinControl),
+                                              C.POINTER(GpuKinLaunch), vp, i32]),
             "kin_model_new": (vp, []),
             "kin_model_air": (vp, []),
             "kin_model_free": (None, [vp]),

@@ -74,6 +74,7 @@ def build(force: bool = False, jobs: int | None = None) -> str:
         ("kern_table_p2.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=2", "-c", os.path.join(CSRC, "kern_table.cu")]),
         ("kern_probe.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "kern_probe.cu")]),
         ("gpu_module.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "gpu_module.cu")]),
+        ("static_scratch.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "static_scratch.cu")]),
         ("mech.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "mech.cpp")]),
         ("host_api.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "host_api.cpp")]),
     ]

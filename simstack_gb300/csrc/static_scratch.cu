@@ -1,0 +1,218 @@
+// gpu_kin_advance_noalloc: the persistent work-queue advance for callers that
+// cannot allocate device memory.
+//
+// Who needs it: a caller that owns all device memory through its own arena
+// (SimStack's platform layer hands the simulation one fixed block and never
+// allocates again), a caller recording the advance into a CUDA graph (an
+// allocation cannot be captured), or a caller on a real-time loop that may not
+// take cudaMalloc's implicit device-wide synchronisation. gpu_init allocates
+// the module's arena and scratch, so such callers cannot use the regular
+// entry points; this one needs no gpu_init at all.
+//
+// What it uses instead: the queue kernel's scratch -- the work-queue cursor,
+// the bounded-wait error flag and, for mechanisms without generated code, the
+// staged copy of the mechanism tables -- lives in g_kin_static_scratch below,
+// a file-scope device array of kStaticScratchBytes (32 KiB) that every GPU
+// holds from the moment the library is loaded until the process exits. The
+// kernels are the ones gpu_kin_advance_queue launches; only where their
+// scratch lives differs. Inputs and outputs are the caller's zone block, as
+// for every other advance.
+
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include "../../include/simstack_gpu.h"
+#include "kin_kernels.cuh"
+#include "kin_table.cuh"
+#include "mech.h"
+
+namespace sgb {
+cudaError_t launch_air_p0(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t launch_air_p1(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t launch_air_p2(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_air_p0(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t occupancy_air_p1(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t occupancy_air_p2(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t launch_table_p0(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t launch_table_p1(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t launch_table_p2(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_table_p0(uint32_t, uint32_t, size_t, int *);
+cudaError_t occupancy_table_p1(uint32_t, uint32_t, size_t, int *);
+cudaError_t occupancy_table_p2(uint32_t, uint32_t, size_t, int *);
+uint64_t air_ops_signature();
+}   // namespace sgb
+
+using namespace sgb;
+
+namespace {
+
+// Layout: queue cursor at +0, error flag at +128 (separate 128-byte lines),
+// mechanism table image (table-driven kernels only) at +256.
+constexpr uint32_t kStaticScratchBytes = 32768;
+constexpr uint32_t kQueueHeaderBytes = 256;
+static_assert(kQueueHeaderBytes + kTableBytes <= kStaticScratchBytes, "table image must fit the static scratch");
+
+static __device__ __align__(256) unsigned char g_kin_static_scratch[kStaticScratchBytes];
+
+// Device address of g_kin_static_scratch per device ordinal, looked up once
+// per device with that device current (the array's name in host code is only
+// a host-side stand-in and must never be passed to a kernel).
+constexpr int kMaxDevices = 64;
+unsigned char *g_scratch_ptr[kMaxDevices];
+
+cudaError_t scratch_for_current_device(unsigned char **out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+    if (!g_scratch_ptr[dev]) {
+        void *p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_kin_static_scratch);
+        if (e != cudaSuccess) return e;
+        g_scratch_ptr[dev] = (unsigned char *)p;
+    }
+    *out = g_scratch_ptr[dev];
+    return cudaSuccess;
+}
+
+bool method_is_rodas3(const KinMethod *m) {
+    KinMethod r = method_coefficients(2);
+    return m->stages == r.stages && m->order == r.order && memcmp(m->a, r.a, sizeof(r.a)) == 0 &&
+           memcmp(m->c, r.c, sizeof(r.c)) == 0 && memcmp(m->m, r.m, sizeof(r.m)) == 0 &&
+           memcmp(m->e, r.e, sizeof(r.e)) == 0 && m->gamma0 == r.gamma0 && memcmp(m->new_f, r.new_f, sizeof(r.new_f)) == 0;
+}
+
+// The table kernels trust every index: reject records that would read outside them.
+bool mech_tables_valid(const KinMech *mech, const KinMethod *method) {
+    const uint32_t n = mech->species_count, nnz = mech->nnz;
+    if (n == 0 || n > KIN_MAX_SPECIES || mech->reaction_count > KIN_MAX_REACTIONS || nnz > KIN_MAX_NNZ ||
+        mech->lu_div_count > KIN_MAX_LU_DIV || mech->lu_sub_count > KIN_MAX_LU_SUB || method->stages < 2 ||
+        method->stages > KIN_MAX_STAGES)
+        return false;
+    if (mech->div_begin[n] != mech->lu_div_count || mech->lower_begin[n] > KIN_MAX_NNZ || mech->upper_begin[n] > KIN_MAX_NNZ)
+        return false;
+    for (uint32_t i = 0; i < n; ++i)
+        if (mech->diag[i] >= nnz || mech->div_begin[i] > mech->div_begin[i + 1] ||
+            mech->lower_begin[i] > mech->lower_begin[i + 1] || mech->upper_begin[i] > mech->upper_begin[i + 1])
+            return false;
+    for (uint32_t d = 0; d < mech->lu_div_count; ++d) {
+        const KinLuDiv &v = mech->lu_div[d];
+        if (v.ik >= nnz || v.kk >= nnz || v.sub_begin > v.sub_end || v.sub_end > mech->lu_sub_count) return false;
+    }
+    for (uint32_t s = 0; s < mech->lu_sub_count; ++s)
+        if (mech->lu_sub[s].ij >= nnz || mech->lu_sub[s].kj >= nnz) return false;
+    for (uint32_t e = 0; e < mech->lower_begin[n]; ++e)
+        if (mech->lower[e].index >= nnz || mech->lower[e].col >= n) return false;
+    for (uint32_t e = 0; e < mech->upper_begin[n]; ++e)
+        if (mech->upper[e].index >= nnz || mech->upper[e].col >= n) return false;
+    for (uint32_t r = 0; r < mech->reaction_count; ++r) {
+        const KinReaction &rx = mech->reactions[r];
+        if (rx.reactant_count > KIN_MAX_REACTANTS || rx.net_count > KIN_MAX_NET) return false;
+        for (uint32_t p = 0; p < rx.reactant_count; ++p) {
+            if (rx.reactant[p] >= n) return false;
+            for (uint32_t e = 0; e < rx.net_count; ++e)
+                if (rx.jac_index[p][e] >= nnz) return false;
+        }
+        for (uint32_t e = 0; e < rx.net_count; ++e)
+            if (rx.net_species[e] >= n) return false;
+    }
+    return true;
+}
+
+}   // namespace
+
+// Advances lanes [0, lane_count) of a zone block with the persistent work-queue
+// kernel, allocating no device memory. See include/simstack_gpu.h.
+SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *method, const KinControl *control,
+                                        const GpuKinLaunch *L, void *stream, int32_t wait) {
+    if (!mech || !method || !control || !L) return (int32_t)cudaErrorInvalidValue;
+    if (L->precision > 2 || L->padded == 0 || L->lane_count > L->padded) return (int32_t)cudaErrorInvalidValue;
+    if (!(L->duration >= 0.0) || L->duration > 1.0e300) return (int32_t)cudaErrorInvalidValue;
+    if (!L->y || !L->h || !L->steps || !L->rejects || !L->pulses || !L->failed || !L->k || !L->src || !L->pulse ||
+        !L->period || !L->pulse_first || !L->pulse_count)
+        return (int32_t)cudaErrorInvalidValue;
+    if (!mech_tables_valid(mech, method)) return (int32_t)cudaErrorInvalidValue;
+    const bool generated = fnv1a(mech, sizeof(KinMech)) == air_ops_signature() && method_is_rodas3(method);
+
+    // scratch this call needs: the queue header, plus the table image for the table-driven kernels
+    const uint64_t needed = kQueueHeaderBytes + (generated ? 0u : kTableBytes);
+    if (needed > kStaticScratchBytes) return (int32_t)cudaErrorMemoryAllocation;   // needs more than the static array holds
+
+    unsigned char *scratch = nullptr;
+    cudaError_t e = scratch_for_current_device(&scratch);
+    if (e != cudaSuccess) return (int32_t)e;
+    cudaStream_t s = (cudaStream_t)stream;
+
+    // the cursor and the error flag must start at zero; the array keeps the last call's contents
+    e = cudaMemsetAsync(scratch, 0, kQueueHeaderBytes, s);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (!generated) {
+        // staged once per call from a host image (pageable: the copy is staged before this call returns)
+        static unsigned char image[kTableBytes];
+        memset(image, 0, sizeof(image));
+        memcpy(image, mech, sizeof(KinMech));
+        unsigned char *mask = image + kJacMaskOffset;
+        const uint32_t n = mech->species_count;
+        for (uint32_t i = 0; i < n; ++i) mask[mech->diag[i] >> 3] |= (unsigned char)(1u << (mech->diag[i] & 7));
+        for (uint32_t r = 0; r < mech->reaction_count; ++r) {
+            const KinReaction &rx = mech->reactions[r];
+            for (uint32_t p = 0; p < rx.reactant_count; ++p)
+                for (uint32_t q = 0; q < rx.net_count; ++q)
+                    mask[rx.jac_index[p][q] >> 3] |= (unsigned char)(1u << (rx.jac_index[p][q] & 7));
+        }
+        e = cudaMemcpyAsync(scratch + kQueueHeaderBytes, image, kTableBytes, cudaMemcpyHostToDevice, s);
+        if (e != cudaSuccess) return (int32_t)e;
+    }
+
+    DevArgs A;
+    memset(&A, 0, sizeof(A));
+    A.y = L->y; A.h = L->h; A.steps = L->steps; A.rejects = L->rejects; A.pulses = L->pulses; A.failed = L->failed;
+    A.k = L->k; A.src = L->src; A.pulse = L->pulse; A.period = L->period;
+    A.pulse_first = L->pulse_first; A.pulse_count = L->pulse_count;
+    A.padded = L->padded;
+    A.lanes = L->lane_count ? L->lane_count : L->padded;
+    A.duration = L->duration;
+    A.ctl = *control;
+    memcpy(A.ma, method->a, sizeof(A.ma));
+    memcpy(A.mc, method->c, sizeof(A.mc));
+    memcpy(A.mm, method->m, sizeof(A.mm));
+    memcpy(A.me, method->e, sizeof(A.me));
+    A.gamma0 = method->gamma0;
+    memcpy(A.new_f, method->new_f, sizeof(A.new_f));
+    A.stages = method->stages;
+    A.order = method->order;
+    A.ir_sweeps = 1;
+    A.cursor = (uint32_t *)scratch;
+    A.error_flag = (uint32_t *)(scratch + 128);
+    A.tables = scratch + kQueueHeaderBytes;
+    A.table_bytes = kTableBytes;
+    if (A.lanes == 0) return 0;
+
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaGetDevice(&dev);
+    e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return (int32_t)e;
+    Shape sh;
+    sh.kind = 1;
+    sh.block = 128;
+    sh.variant = 0;
+    sh.smem = generated ? 0 : kTableBytes;
+    const uint32_t p = L->precision;
+    if (generated) e = p == 0 ? occupancy_air_p0(1, 0, sh.block, &per_sm) : p == 1 ? occupancy_air_p1(1, 0, sh.block, &per_sm)
+                                                                                  : occupancy_air_p2(1, 0, sh.block, &per_sm);
+    else e = p == 0 ? occupancy_table_p0(1, sh.block, sh.smem, &per_sm) : p == 1 ? occupancy_table_p1(1, sh.block, sh.smem, &per_sm)
+                                                                              : occupancy_table_p2(1, sh.block, sh.smem, &per_sm);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (per_sm < 1) per_sm = 1;
+    const uint32_t resident = (uint32_t)per_sm * (uint32_t)sms, needed_ctas = (A.lanes + sh.block - 1) / sh.block;
+    sh.grid = resident < needed_ctas ? resident : needed_ctas;
+    if (generated) e = p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : launch_air_p2(sh, A, s);
+    else e = p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : launch_table_p2(sh, A, s);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (!wait) return 0;
+    uint32_t flag = 0;
+    e = cudaMemcpyAsync(&flag, scratch + 128, sizeof(flag), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return (int32_t)e;
+    return flag ? (int32_t)cudaErrorTimeout : (int32_t)cudaGetLastError();
+}
