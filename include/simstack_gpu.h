@@ -260,6 +260,7 @@ SGB_API uint32_t kin_model_add_reaction(KinModelHandle *model, const char *equat
                                         int32_t ref);
 SGB_API int32_t kin_model_finalize(KinModelHandle *model); /* 0 ok, else see kin_model_error */
 SGB_API const char *kin_model_error(const KinModelHandle *model);
+SGB_API int32_t kin_model_equation(const KinModelHandle *model, uint32_t r, char *out, uint32_t size); /* 0 if out of range */
 /* counts[0..6] = species, reactions, nnz, lu divisions, lu updates, lower, upper */
 SGB_API void kin_model_counts(const KinModelHandle *model, uint64_t *counts);
 /* Reference-layout tables; cudaErrorInvalidValue (1) if the mechanism exceeds them. */

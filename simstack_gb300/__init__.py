@@ -149,6 +149,7 @@ def lib() -> C.CDLL:
             "kin_model_add_reaction": (u32, [vp, C.c_char_p, i32, C.POINTER(d), i32]),
             "kin_model_finalize": (i32, [vp]),
             "kin_model_error": (C.c_char_p, [vp]),
+            "kin_model_equation": (i32, [vp, u32, C.c_char_p, u32]),
             "kin_model_counts": (None, [vp, C.POINTER(u64)]),
             "kin_model_kinmech": (i32, [vp, C.POINTER(KinMech)]),
             "kin_mech_signature": (u64, [C.POINTER(KinMech)]),
@@ -255,6 +256,13 @@ class Model:
         k = np.zeros(max(self.R, 1))
         lib().kin_model_rate_constants(self.h, T, M, _p(k))
         return k[: self.R]
+
+
+def model_equation(model: Model, r: int) -> str:
+    buf = C.create_string_buffer(128)
+    if not lib().kin_model_equation(model.h, r, buf, 128):
+        raise IndexError(r)
+    return buf.value.decode()
 
 
 def kinmech_bytes(km: KinMech) -> bytes:

@@ -48,6 +48,13 @@ SGB_API uint32_t kin_model_add_reaction(KinModelHandle *h, const char *equation,
 
 SGB_API int32_t kin_model_finalize(KinModelHandle *h) { return h->model.finalize() ? 0 : 1; }
 
+// Equation text of reaction r (NUL-terminated, truncated to size); 0 if r is out of range.
+SGB_API int32_t kin_model_equation(const KinModelHandle *h, uint32_t r, char *out, uint32_t size) {
+    if (r >= h->model.R() || size == 0) return 0;
+    snprintf(out, size, "%s", h->model.reactions[r].equation.c_str());
+    return 1;
+}
+
 SGB_API const char *kin_model_error(const KinModelHandle *h) { return h->model.error.c_str(); }
 
 SGB_API void kin_model_counts(const KinModelHandle *h, uint64_t *c) {
