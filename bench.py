@@ -53,6 +53,8 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--profile-case", choices=["f64", "mixed", "f32"], default=None,
+                    help="one queue-kernel advance of --cells x --duration at this precision, then exit (ncu captures)")
     return ap.parse_args()
 
 
@@ -428,9 +430,26 @@ def run_ours(args):
     grp.close()
 
 
+def run_profile_case(args):
+    """One advance on cuda:0 for an ncu capture: the persistent queue kernel, default tuning."""
+    import simstack_gb300 as sg
+
+    prec = {"f64": 0, "f32": 1, "mixed": 2}[args.profile_case]
+    mod = sg.Module(0, 2 * sg.ZoneBlock(17, 44, args.cells).nbytes + (64 << 20))
+    ctl = sg.control() if prec != 1 else sg.control(rtol=1e-3, atol=1e8, max_steps=20000)
+    mod.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), ctl)
+    z = sg.air_cells(args.cells, seed=args.seed)
+    ms = mod.integrate(z, args.duration, precision=prec, queue=True)
+    steps = float(z["steps"][:args.cells].sum() + z["rejects"][:args.cells].sum())
+    print(json.dumps({"case": args.profile_case, "cells": args.cells, "duration_s": args.duration, "kernel_ms": ms,
+                      "cell_steps": steps}))
+
+
 if __name__ == "__main__":
     a = parse()
-    if a.impl == "reference":
+    if a.profile_case:
+        run_profile_case(a)
+    elif a.impl == "reference":
         run_reference(a)
     else:
         run_ours(a)
