@@ -187,10 +187,13 @@ SGB_API int32_t gpu_kin_set_mode(uint32_t mode);
  * warps next to stiff ones. Same results as gpu_kin_advance for every lane. */
 SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_ms);
 
-/* Launch tuning. kind: 0 static one-cell-per-thread, 1 persistent queue.
- * block = threads per CTA (multiple of 32, <= 128), chunk = resident CTAs per
- * SM for the queue kernel (0: as many as fit), variant = compiled
- * register-budget variant (0: up to 255 registers, 1: 128).
+/* Launch tuning. kind: 0 static one-cell-per-thread, 1 persistent queue
+ * (warp-synchronous), 2 persistent queue with the CTA's warps stepping
+ * together (default). block = threads per CTA (multiple of 32; <= 128, or
+ * 256 with variant 2), chunk = resident CTAs per SM for the queue kernels
+ * (0: as many as fit), variant = compiled register-budget variant (0: up to
+ * 255 registers at 128 threads, 1: 128 registers, 2: 255 registers at 256
+ * threads, kind 2 only).
  * gpu_kin_autotune times candidates on the given launch (which it advances
  * repeatedly on a scratch copy it restores) and keeps the fastest. */
 typedef struct GpuKinTuning {

@@ -57,7 +57,7 @@ struct Module {
 };
 Module g;
 
-const GpuKinTuning kDefaultTuning = {1u, 128u, 0u, 0u, 0.0f};
+const GpuKinTuning kDefaultTuning = {2u, 128u, 0u, 0u, 0.0f};   // CTA-synchronous queue, 128 threads, 255 registers
 
 bool is_rodas3(const KinMethod *m) {
     KinMethod r = method_coefficients(2);
@@ -111,7 +111,7 @@ cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &
     s.smem = g.generated ? 0 : kTableBytes;
     if (t.kind == 0) {
         s.grid = (A.lanes + t.block - 1) / t.block;
-    } else {
+    } else {   // queue kernels: persistent grid, the cursor starts at zero
         int per_sm = 0;
         cudaError_t e = occupancy(prec, t, &per_sm);
         if (e != cudaSuccess) return e;
@@ -425,13 +425,19 @@ SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_
     uint32_t p = launch ? launch->precision : 0;
     if (p > 2) return (int32_t)cudaErrorInvalidValue;
     GpuKinTuning t = g.tuning[p];
-    t.kind = 1;
+    if (t.kind == 0) {   // a static tuning: run the CTA-synchronous queue at its default shape
+        t.kind = 2;
+        t.block = 128;
+        t.variant = 0;
+        t.chunk = 0;
+    }
     return (int32_t)advance_sync(launch, t, kernel_ms);
 }
 
 SGB_API int32_t gpu_kin_set_tuning(const GpuKinTuning *t) {
-    if (!t || t->kind > 1 || t->block == 0 || t->block > 128 || (t->block & 31) || t->variant > 1 || t->chunk > 64)
-        return (int32_t)cudaErrorInvalidValue;
+    if (!t || t->kind > 2 || t->block == 0 || (t->block & 31) || t->variant > 2 || t->chunk > 64) return (int32_t)cudaErrorInvalidValue;
+    const uint32_t max_block = t->variant == 2 ? 256u : 128u;   // the variant's __launch_bounds__
+    if (t->block > max_block || (t->variant == 2 && t->kind != 2)) return (int32_t)cudaErrorInvalidValue;
     for (int p = 0; p < 3; ++p) g.tuning[p] = *t;
     return 0;
 }
@@ -448,7 +454,7 @@ SGB_API int32_t gpu_kin_get_tuning(uint32_t precision, GpuKinTuning *t) {
 SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuKinTuning *best) {
     cudaError_t e = check_launch(launch);
     if (e != cudaSuccess) return (int32_t)e;
-    if (kind > 1) return (int32_t)cudaErrorInvalidValue;
+    if (kind > 2) return (int32_t)cudaErrorInvalidValue;
     const uint64_t P = launch->padded, n = g.mech.species_count;
     const uint64_t bytes_y = n * P * sizeof(double), bytes_v = P * sizeof(double);
     double *save = nullptr;
@@ -470,9 +476,13 @@ SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuK
     struct Cand { uint32_t block, variant, ctas; };
     const Cand cands[] = {{32, 0, 0}, {64, 0, 0}, {128, 0, 0}, {64, 1, 0}, {128, 1, 0},
                           {128, 0, 1}, {64, 0, 2}, {64, 0, 3}, {128, 1, 2}, {128, 1, 3}};
+    const Cand sync_cands[] = {{256, 2, 1}, {128, 0, 2}, {128, 0, 1}, {128, 1, 3}, {128, 1, 4}};
     GpuKinTuning winner = g.tuning[launch->precision];
     winner.ms = 1e30f;
-    for (const Cand &c : cands) {
+    const Cand *list = kind == 2 ? sync_cands : cands;
+    const size_t count = kind == 2 ? sizeof(sync_cands) / sizeof(Cand) : sizeof(cands) / sizeof(Cand);
+    for (size_t ci = 0; ci < count; ++ci) {
+        const Cand &c = list[ci];
         if (e != cudaSuccess) break;
         if (kind == 0 && c.ctas != 0) continue;
         {

@@ -385,7 +385,12 @@ struct Lane {
     }
 
     // One pass of kin_integrate's step loop (kin_solver.h:216-311) for an active lane.
-    __device__ __forceinline__ void attempt(const DevArgs &A) {
+    // kSync: called by every thread of the CTA together (the CTA-synchronous
+    // kernel); barriers between the phases keep the CTA's warps on the same
+    // stretch of straight-line code. commit = false: the lane has no cell this
+    // round; it computes on its last state and keeps none of the results.
+    template <bool kSync = false>
+    __device__ __forceinline__ void attempt(const DevArgs &A, bool commit = true) {
         const T zero = (T)0.0, one = (T)1.0;
         const uint32_t nn = n();
         const T h_min = (T)A.ctl.h_min, rtol = (T)A.ctl.rtol, atol = (T)A.ctl.atol;
@@ -412,9 +417,11 @@ struct Lane {
             ops.fun(k, src, at, fcn);
             ops.neg_jac(k, at, lu);
         }
+        if constexpr (kSync) __syncthreads();
         T ghinv = one / (hs * (T)M::gamma0(A));
         if constexpr (kMixed) ops.factor((float)ghinv, lu);
         else ops.factor((Cf)ghinv, lu);
+        if constexpr (kSync) __syncthreads();
         T hinv = one / hs;
 
         bool fcn_at_y = true;   // fcn (plain paths) holds f at the step-start point
@@ -487,6 +494,7 @@ struct Lane {
             } else {
                 ops.solve(lu, K[st]);
             }
+            if constexpr (kSync) __syncthreads();
         }
 
         // y_new into ytmp and the weighted RMS error (kin_solver.h:263-280)
@@ -521,6 +529,7 @@ struct Lane {
             ok = true;
             fac = one;
         }
+        if (!commit) return;
         if (ok) {
             for (int s = 0; s < N; ++s) {
                 if (s >= (int)nn) break;

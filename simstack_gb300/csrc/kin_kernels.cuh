@@ -22,6 +22,7 @@ namespace sgb {
 template <int V> struct Budget;
 template <> struct Budget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
 template <> struct Budget<1> { static constexpr int kThreads = 128, kMinBlocks = 4; };
+template <> struct Budget<2> { static constexpr int kThreads = 256, kMinBlocks = 1; };
 
 // Both kernels keep every lane of a warp in the loop until the whole warp is
 // out of work, and vote (__any_sync) once per iteration: the vote is a
@@ -88,6 +89,49 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
     }
 }
 
+// CTA-synchronous persistent queue: like kin_queue_kernel, but the whole CTA
+// votes (__syncthreads_or) and runs every step attempt together, with
+// barriers between its phases, so the CTA's warps fetch the same stretch of
+// the straight-line step code instead of one stretch each (the step code is
+// far larger than the instruction caches). Lanes without a cell compute on
+// their last state and commit nothing; a lane that never had one starts from
+// a copy of cell 0.
+template <class Ops, class M, int PREC, int V>
+__global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_queue_cta_kernel(const __grid_constant__ DevArgs A) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    Lane<Ops, M, PREC> L;
+    if (!L.ops.init(A, smem)) {
+        if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
+        return;
+    }
+    if (A.lanes == 0) return;
+    L.load(A, 0);   // a finite state for lanes that never get a cell
+    bool have = false, exhausted = false;
+    uint32_t cell = 0;
+    for (;;) {
+        bool need = false;
+        while (!exhausted) {
+            if (!have) {
+                cell = atomicAdd(A.cursor, 1u);
+                if (cell >= A.lanes) {
+                    exhausted = true;
+                    break;
+                }
+                L.load(A, cell);
+                have = true;
+            }
+            if (L.settle(A, cell)) {
+                need = true;
+                break;
+            }
+            L.store(A, cell);
+            have = false;
+        }
+        if (!__syncthreads_or(need)) break;
+        L.template attempt<true>(A, need);
+    }
+}
+
 // Launch shape chosen by the host (module tuning or the autotuner).
 struct Shape {
     uint32_t kind;      // 0 static, 1 queue
@@ -100,6 +144,10 @@ struct Shape {
 // kVariants: how many register-budget variants are instantiated (1: variant 0 only).
 template <class Ops, class M, int PREC, int kVariants>
 void (*kernel_for(uint32_t kind, uint32_t variant))(DevArgs) {
+    if (kind == 2) {   // CTA-synchronous queue: 128 threads (variant 0) or 256 threads, one CTA per SM (variant 2)
+        if (kVariants > 1 && variant == 2) return kin_queue_cta_kernel<Ops, M, PREC, (kVariants > 1 ? 2 : 0)>;
+        return kin_queue_cta_kernel<Ops, M, PREC, 0>;
+    }
     if (kVariants > 1 && variant == 1)
         return kind == 0 ? kin_static_kernel<Ops, M, PREC, (kVariants > 1 ? 1 : 0)> : kin_queue_kernel<Ops, M, PREC, (kVariants > 1 ? 1 : 0)>;
     return kind == 0 ? kin_static_kernel<Ops, M, PREC, 0> : kin_queue_kernel<Ops, M, PREC, 0>;

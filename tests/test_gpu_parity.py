@@ -28,11 +28,12 @@ def assert_bits(a, b, names=STATE):
         assert x.tobytes() == y.tobytes(), f"{name}: {np.count_nonzero(x != y)} entries differ"
 
 
-@pytest.mark.parametrize("kind", [0, 1], ids=["static", "queue"])
-def test_f64_bit_identical_config1(module, oracle_lib, kind):
+@pytest.mark.parametrize("kind,block,variant", [(0, 128, 0), (1, 128, 0), (2, 128, 0), (2, 256, 2)],
+                         ids=["static", "queue", "cta-queue", "cta-queue-256"])
+def test_f64_bit_identical_config1(module, oracle_lib, kind, block, variant):
     """4,096-cell config-1 inputs (1 s, rtol 1e-4): every output bit equal to the oracle."""
     module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
-    module.set_tuning(kind=kind, block=128, variant=0)
+    module.set_tuning(kind=kind, block=block, variant=variant)
     z = sg.air_cells(4096, seed=1)
     ref = z.copy()
     module.integrate(z, 1.0, precision=0)
@@ -210,7 +211,7 @@ def test_mixed_matches_model(module, oracle_lib, method):
     """The GPU mixed kernel (generated code for Rodas3, table walk otherwise)
     performs exactly the operations of the oracle's model of the mixed path."""
     module.set_mech(sg.Model.air().kinmech(), sg.method(method), sg.control())
-    for kind in (0, 1):
+    for kind in (0, 1, 2):
         module.set_tuning(kind=kind)
         z = sg.air_cells(1024, seed=6)
         ref = z.copy()
