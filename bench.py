@@ -53,6 +53,9 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--workload", choices=["config2", "config1", "config3"], default="config2",
+                    help="config2 (default, the headline): 1,048,576 cells x 10 s; config1: 4,096 cells x 1 s; "
+                         "config3: uneven stiffness, 262,144 cells x 60 s with a discharge source, static vs queue")
     ap.add_argument("--profile-case", choices=["f64", "mixed", "f32"], default=None,
                     help="one queue-kernel advance of --cells x --duration at this precision, then exit (ncu captures)")
     return ap.parse_args()
@@ -430,6 +433,58 @@ def run_ours(args):
     grp.close()
 
 
+# Config 3: the shipped source model's per-second discharge source at a power
+# drawn log-uniform over 3 decades from P0 (W/cm^3); P0 = 1e-2 gives accepted
+# steps from ~150 to ~2,700 per cell over 60 s on these initial states (p50 ~280),
+# measured on the oracle (64-cell sample, seed 3).
+CONFIG3_P0 = 1e-2
+
+
+def run_config3(args):
+    import simstack_gb300 as sg
+
+    cells = args.cells if args.cells != (1 << 20) else 262144
+    duration = args.duration if args.duration != 10.0 else 60.0
+    L = sg.lib()
+    z = sg.air_cells(cells, seed=args.seed)
+    power = sg.air_source(z, seed=args.seed, P0=CONFIG3_P0, decades=3.0)
+    mod = sg.Module(0, 3 * z.nbytes + (256 << 20))
+    mod.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    pristine = mod.upload(z)
+    work = mod.alloc(z.nbytes)
+    launch = z.launch(work, 0, duration)
+    results = {}
+    for prec in (0, 2):
+        launch.precision = prec
+        for kind in (0, 2):
+            sg.check(L.gpu_copy_on_device(work, pristine, z.nbytes), "copy")
+            t = mod.autotune(launch, kind=kind)
+            times = []
+            for it in range(args.warmup + args.steps):
+                sg.check(L.gpu_copy_on_device(work, pristine, z.nbytes), "copy")
+                ms = mod.advance(launch)
+                if it >= args.warmup:
+                    times.append(ms)
+            ms = float(np.mean(times))
+            results[f"{'f64' if prec == 0 else 'mixed'}_{'static' if kind == 0 else 'queue'}"] = {
+                "ms": ms, "value": cells / (ms * 1e-3), "tuning": {"block": t.block, "variant": t.variant, "ctas_per_sm": t.chunk}}
+    zc = z.copy()
+    mod.download(zc, work)
+    steps = zc["steps"][:cells]
+    line = {"metric": "cell-integrations/s", "value": results["mixed_queue"]["value"], "unit": "cell-integrations/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": results["mixed_queue"]["ms"],
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"uneven stiffness: shipped mechanism, {cells} cells x {duration:g} s, averaged discharge "
+                                   f"source at P0 x 10^U[0,3] W/cm^3, P0 = {CONFIG3_P0:g}",
+                       "power_W_cm3": [float(power[:cells].min()), float(power[:cells].max())]},
+            "accepted_steps_per_cell": {"min": float(steps.min()), "p50": float(np.median(steps)),
+                                        "p99": float(np.quantile(steps, 0.99)), "max": float(steps.max())},
+            "kernels": results,
+            "queue_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue"]["ms"],
+                                        "mixed": results["mixed_static"]["ms"] / results["mixed_queue"]["ms"]}}
+    print(json.dumps(line))
+
+
 def run_profile_case(args):
     """One advance on cuda:0 for an ncu capture: the persistent queue kernel, default tuning."""
     import simstack_gb300 as sg
@@ -449,6 +504,8 @@ if __name__ == "__main__":
     a = parse()
     if a.profile_case:
         run_profile_case(a)
+    elif a.workload == "config3" and a.impl == "ours":
+        run_config3(a)
     elif a.impl == "reference":
         run_reference(a)
     else:
