@@ -53,9 +53,11 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--workload", choices=["config2", "config1", "config3"], default="config2",
+    ap.add_argument("--workload", choices=["config2", "config1", "config3", "config5"], default="config2",
                     help="config2 (default, the headline): 1,048,576 cells x 10 s; config1: 4,096 cells x 1 s; "
-                         "config3: uneven stiffness, 262,144 cells x 60 s with a discharge source, static vs queue")
+                         "config3: uneven stiffness, 262,144 cells x 60 s with a discharge source, static vs queue; "
+                         "config5: served requests (Poisson arrivals) with film advection, p50/p99 latency")
+    ap.add_argument("--requests", type=int, default=48, help="config5: requests in the served sample")
     ap.add_argument("--profile-case", choices=["f64", "mixed", "f32"], default=None,
                     help="one queue-kernel advance of --cells x --duration at this precision, then exit (ncu captures)")
     return ap.parse_args()
@@ -485,6 +487,86 @@ def run_config3(args):
     print(json.dumps(line))
 
 
+def serve_sample(seed: int, count: int, rate_hz: float = 200.0):
+    """The served request stream: Poisson arrivals at rate_hz; cells 10^U[log10 1024, log10 65536];
+    horizon 10^U[0, log10 600] s in 1 s coupling steps (log-uniform); channel cells U{256..4096};
+    film speed U[0.01, 0.1] m/s; dx = 0.05 m; shipped mechanism."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate_hz, size=count))
+    cells = np.rint(10.0 ** rng.uniform(np.log10(1024), np.log10(65536), size=count)).astype(int)
+    horizon = np.maximum(1, np.rint(10.0 ** rng.uniform(0.0, np.log10(600.0), size=count))).astype(int)
+    channel = rng.integers(256, 4097, size=count)
+    v = rng.uniform(0.01, 0.1, size=count)
+    return [dict(arrival_s=float(t[i]), cells=int(cells[i]), steps=int(horizon[i]), channel_cells=int(channel[i]),
+                 velocity=float(v[i]), seed=seed * 1000 + i) for i in range(count)]
+
+
+def run_config5(args):
+    """Serving: requests submitted at their arrival times through the public serving API
+    (host arrays in, results back on the host), the engine driven until every request is done."""
+    import time
+
+    import simstack_gb300 as sg
+
+    reqs = serve_sample(args.seed, args.requests)
+    inputs = []
+    for r in reqs:
+        z = sg.air_cells(r["cells"], seed=r["seed"])
+        inputs.append((np.ascontiguousarray(z["y"][:, :r["cells"]]), np.ascontiguousarray(z["k"][:, :r["cells"]])))
+    out = {}
+    clocks = ClockSampler(0)
+    clock_summary = None
+    for prec, name in ((0, "f64"), (2, "mixed")):
+        with sg.Server() as srv:
+            # warm-up: one small request through the same path (kernel loading, pools)
+            srv.submit(inputs[0][0][:, :1024], inputs[0][1][:, :1024], 1, 256, 0.05, precision=prec)
+            srv.drain(timeout_s=120)
+            ids = [None] * len(reqs)
+            nxt = 0
+            if name == "mixed":
+                clocks.start()
+            t0 = time.monotonic()
+            while True:
+                now = time.monotonic() - t0
+                while nxt < len(reqs) and reqs[nxt]["arrival_s"] <= now:
+                    r = reqs[nxt]
+                    ids[nxt] = srv.submit(inputs[nxt][0], inputs[nxt][1], r["steps"], r["channel_cells"], r["velocity"],
+                                          precision=prec)
+                    nxt += 1
+                running, waiting, _ = srv.progress()
+                if nxt == len(reqs) and running == 0 and waiting == 0:
+                    break
+                time.sleep(1e-4)
+            makespan = time.monotonic() - t0
+            if name == "mixed":
+                clock_summary = clocks.stop()
+            lat = np.array([srv.poll(i)["latency_s"] for i in ids])
+            states = {srv.poll(i)["state"] for i in ids}
+            failed = sum(int(srv.result(i)[2].sum()) for i in ids)
+            st = srv.stats()
+        cell_steps = sum(r["cells"] * r["steps"] for r in reqs)
+        out[name] = {"makespan_s": makespan, "cell_steps_per_s": cell_steps / makespan,
+                     "cell_integrations_per_s": sum(r["cells"] for r in reqs) / makespan,
+                     "latency_s": {"p50": float(np.median(lat)), "p99": float(np.quantile(lat, 0.99)),
+                                   "max": float(lat.max())},
+                     "states": sorted(states), "failed_cells": failed, "graph_launches": st["graph_launches"] - 1,
+                     "peak_device_bytes": st["peak_bytes"]}
+    m = out["mixed"]
+    line = {"metric": "served cell-steps/s (1 s coupling steps)", "value": m["cell_steps_per_s"],
+            "unit": "cell-steps/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": m["makespan_s"] * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"serving: {len(reqs)} requests, Poisson arrivals at 200 req/s (seed {args.seed}), "
+                                   "cells 10^U[log10 1024, log10 65536], horizon 10^U[0, log10 600] s (log-uniform), "
+                                   "channel cells U{256..4096}, v U[0.01, 0.1] m/s, dx 0.05 m, shipped mechanism",
+                       "cell_steps": cell_steps, "requests": len(reqs)},
+            "e2e": {"value": m["cell_steps_per_s"], "unit": "cell-steps/s",
+                    "h2d_bytes_per_step": sum(8 * (3 * 17 + 44 + 8) * ((r["cells"] + 7) // 8 * 8) for r in reqs),
+                    "d2h_bytes_per_step": sum(8 * (17 + 5) * ((r["cells"] + 7) // 8 * 8) for r in reqs)},
+            "gpu_launches": 2 * m["graph_launches"], "clocks": clock_summary, "precisions": out,
+            "mixed_speedup_vs_f64": out["f64"]["makespan_s"] / m["makespan_s"]}
+    print(json.dumps(line))
+
+
 def run_profile_case(args):
     """One advance on cuda:0 for an ncu capture: the persistent queue kernel, default tuning."""
     import simstack_gb300 as sg
@@ -506,6 +588,8 @@ if __name__ == "__main__":
         run_profile_case(a)
     elif a.workload == "config3" and a.impl == "ours":
         run_config3(a)
+    elif a.workload == "config5" and a.impl == "ours":
+        run_config5(a)
     elif a.impl == "reference":
         run_reference(a)
     else:

@@ -244,6 +244,82 @@ SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *me
                                         const GpuKinLaunch *launch, void *stream, int32_t wait);
 
 /* ---------------------------------------------------------------------------
+ * Film advection and the served coupling step (new capability; the reference
+ * has no GPU transport and no serving).
+ *
+ * gpu_advect: explicit upwind transport of a [species][padded] device block
+ * whose first `cells` columns are laid out channel after channel
+ * (`channel_cells` each, at most 4,096): `substeps` sweeps of
+ * x_j = fma(c, x_{j-1} - x_j, x_j), cell 0 of every channel reading
+ * inlet_device[species]. The flux form and the outlet-to-inlet sweep of
+ * src/sim/nft.cpp:1066-1079 in FP64. Enqueued on `stream`.
+ */
+SGB_API int32_t gpu_advect(double *y, uint32_t padded, uint32_t species, uint32_t cells, uint32_t channel_cells,
+                           const double *inlet_device, double courant, uint32_t substeps, void *stream);
+
+/* Serving. A request is a block of cells integrated over `coupling_steps`
+ * steps of `dt` seconds; every step is chemistry over dt (persistent queue
+ * kernel), then film advection (operator split in the order of
+ * src/sim/dbd_scene.cpp:263-265), captured once per request as a CUDA graph
+ * and replayed on the request's own stream. Substeps follow the Courant-0.9
+ * rule of src/sim/nft.cpp:531-536: ceil(dt / (0.9 dx / v)). The inlet of every
+ * channel is the request's cell-0 initial state. State stays in device memory
+ * from admission to completion. Requests are admitted in arrival order while
+ * their device footprint fits the HBM budget; running requests share the GPU
+ * (continuous batching: a request joins as soon as it fits, its steps run
+ * beside everyone else's). Not thread-safe: one host thread drives it. */
+typedef struct GpuServeRequest {
+    const double *y0;          /* host [n][cells] initial state (copied at submit) */
+    const double *k;           /* host [R][cells] rate constants (copied at submit) */
+    uint32_t cells;
+    uint32_t channel_cells;    /* cells per film channel, 1..4096 */
+    uint32_t coupling_steps;
+    uint32_t precision;        /* 0 FP64, 1 f32 Delta lanes, 2 mixed */
+    uint32_t mechanism;        /* 0 the shipped mechanism (generated kernels), 1 the engine's table mechanism */
+    uint32_t reserved;
+    double dt;                 /* coupling step, s */
+    double velocity_m_s;       /* film flow speed */
+    double dx_m;               /* channel cell length */
+} GpuServeRequest;
+
+typedef struct GpuServeStatus {
+    uint32_t state;            /* 0 waiting, 1 running, 2 done, 3 failed, 4 cancelled */
+    int32_t error;             /* cudaError_t of a failed request (cudaErrorTimeout: a bounded wait ran out) */
+    uint32_t steps_completed;
+    uint32_t substeps;
+    double courant;
+    double admit_s;            /* submission to admission, s (-1 while waiting) */
+    double latency_s;          /* submission to completion, s (-1 until finished) */
+} GpuServeStatus;
+
+typedef struct GpuServeStats {
+    uint64_t budget_bytes, in_use_bytes, peak_bytes;
+    uint64_t graph_launches;
+    uint32_t running, waiting, finished, reserved;
+} GpuServeStats;
+
+/* Opens the engine on the current device. Budget: min(hbm_budget_bytes, free
+ * memory - 1 GiB); 0 = all of it. control: NULL = rtol 1e-4, atol 6.022e8. */
+SGB_API int32_t gpu_serve_open(uint64_t hbm_budget_bytes, const KinControl *control);
+/* Table mechanism (mechanism = 1) and its method; only while the engine is empty. */
+SGB_API int32_t gpu_serve_set_mech(const KinMech *mech, const KinMethod *method);
+/* Queues a request; cudaErrorMemoryAllocation if it could never fit the budget. */
+SGB_API int32_t gpu_serve_submit(const GpuServeRequest *request, uint64_t *id);
+/* One scheduling round, non-blocking apart from uploads of newly admitted and
+ * downloads of finished requests: retires finished and cancelled requests,
+ * launches the next step of every running request whose last step completed,
+ * admits waiting requests that fit. */
+SGB_API int32_t gpu_serve_progress(uint32_t *running, uint32_t *waiting, uint32_t *finished);
+SGB_API int32_t gpu_serve_cancel(uint64_t id);
+SGB_API int32_t gpu_serve_poll(uint64_t id, GpuServeStatus *status);
+/* Final state [n][cells], accepted steps and failed flags per cell of a done request. */
+SGB_API int32_t gpu_serve_result(uint64_t id, double *y_out, double *steps_out, double *failed_out);
+/* Drops a finished request's record and result. */
+SGB_API int32_t gpu_serve_forget(uint64_t id);
+SGB_API int32_t gpu_serve_stats(GpuServeStats *stats);
+SGB_API int32_t gpu_serve_close(void);
+
+/* ---------------------------------------------------------------------------
  * Host-side mechanism compiler: src/sim/kinetics/kin_build.cpp:199-365 and
  * air_mech.cpp:30-108, 205-276. Builds the reference-layout KinMech (same
  * pattern, pivot order and bytes as kin_mech_finalize), rate constants and

@@ -87,6 +87,24 @@ class GpuKinTuning(C.Structure):
                 ("ms", C.c_float)]
 
 
+class GpuServeRequest(C.Structure):
+    _fields_ = [("y0", C.c_void_p), ("k", C.c_void_p), ("cells", C.c_uint32), ("channel_cells", C.c_uint32),
+                ("coupling_steps", C.c_uint32), ("precision", C.c_uint32), ("mechanism", C.c_uint32),
+                ("reserved", C.c_uint32), ("dt", C.c_double), ("velocity_m_s", C.c_double), ("dx_m", C.c_double)]
+
+
+class GpuServeStatus(C.Structure):
+    _fields_ = [("state", C.c_uint32), ("error", C.c_int32), ("steps_completed", C.c_uint32),
+                ("substeps", C.c_uint32), ("courant", C.c_double), ("admit_s", C.c_double), ("latency_s", C.c_double)]
+
+
+class GpuServeStats(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("in_use_bytes", C.c_uint64), ("peak_bytes", C.c_uint64),
+                ("graph_launches", C.c_uint64), ("running", C.c_uint32), ("waiting", C.c_uint32),
+                ("finished", C.c_uint32), ("reserved", C.c_uint32)]
+
+
+assert C.sizeof(GpuServeRequest) == 64 and C.sizeof(GpuServeStatus) == 40 and C.sizeof(GpuServeStats) == 48
 assert C.sizeof(KinMech) == 30044 and C.sizeof(KinMethod) == 200 and C.sizeof(KinControl) == 56
 assert C.sizeof(GpuKinLaunch) == 120 and C.sizeof(GpuInfo) == 168
 
@@ -142,6 +160,17 @@ def lib() -> C.CDLL:
             "gpu_copy_on_device": (i32, [vp, vp, u64]),
             "gpu_kin_advance_noalloc": (i32, [C.POINTER(KinMech), C.POINTER(KinMethod), C.POINTER(KinControl),
                                               C.POINTER(GpuKinLaunch), vp, i32]),
+            "gpu_advect": (i32, [vp, u32, u32, u32, u32, vp, d, u32, vp]),
+            "gpu_serve_open": (i32, [u64, C.POINTER(KinControl)]),
+            "gpu_serve_set_mech": (i32, [C.POINTER(KinMech), C.POINTER(KinMethod)]),
+            "gpu_serve_submit": (i32, [C.POINTER(GpuServeRequest), C.POINTER(u64)]),
+            "gpu_serve_progress": (i32, [C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
+            "gpu_serve_cancel": (i32, [u64]),
+            "gpu_serve_poll": (i32, [u64, C.POINTER(GpuServeStatus)]),
+            "gpu_serve_result": (i32, [u64, vp, vp, vp]),
+            "gpu_serve_forget": (i32, [u64]),
+            "gpu_serve_stats": (i32, [C.POINTER(GpuServeStats)]),
+            "gpu_serve_close": (i32, []),
             "kin_model_new": (vp, []),
             "kin_model_air": (vp, []),
             "kin_model_free": (None, [vp]),
@@ -546,3 +575,88 @@ def dbd_prepare_source(z: ZoneBlock, pulsed: bool, t0: float, t1: float) -> None
 
 def dbd_commit_pulses(z: ZoneBlock) -> None:
     z.pulse_index += z["pulse_count"]
+
+
+SERVE_STATES = ("waiting", "running", "done", "failed", "cancelled")
+
+
+class Server:
+    """The serving engine (gpu_serve_*): requests of cells integrated over 1 s
+    coupling steps of chemistry + film advection, admitted while they fit the
+    HBM budget, state device-resident until done. One host thread drives it
+    through progress()."""
+
+    def __init__(self, budget_bytes: int = 0, ctl: KinControl | None = None):
+        self._ctl = ctl if ctl is not None else control()
+        check(lib().gpu_serve_open(budget_bytes, C.byref(self._ctl)), "gpu_serve_open")
+        self._species = {}
+
+    def set_mech(self, km: KinMech, meth: KinMethod | None = None) -> None:
+        meth = meth if meth is not None else method("rodas3")
+        self._mech = (km, meth)
+        check(lib().gpu_serve_set_mech(C.byref(km), C.byref(meth)), "gpu_serve_set_mech")
+        self._table_shape = (int(km.species_count), int(km.reaction_count))
+
+    def submit(self, y0: np.ndarray, k: np.ndarray, coupling_steps: int, channel_cells: int, velocity_m_s: float,
+               dx_m: float = 0.05, dt: float = 1.0, precision: int = 0, mechanism: int = 0) -> int:
+        y0 = np.ascontiguousarray(y0, dtype=np.float64)
+        k = np.ascontiguousarray(k, dtype=np.float64)
+        n, R = (17, 44) if mechanism == 0 else getattr(self, "_table_shape", (0, 0))
+        if mechanism in (0, 1) and (y0.shape[0] != n or k.shape != (R, y0.shape[1])):
+            raise ValueError(f"request arrays {y0.shape} / {k.shape} do not match the mechanism ({n} species, {R} reactions)")
+        q = GpuServeRequest(_p(y0), _p(k), y0.shape[1], channel_cells, coupling_steps, precision, mechanism, 0, dt,
+                            velocity_m_s, dx_m)
+        rid = C.c_uint64()
+        check(lib().gpu_serve_submit(C.byref(q), C.byref(rid)), "gpu_serve_submit")
+        self._species[rid.value] = (y0.shape[0], y0.shape[1])
+        return rid.value
+
+    def progress(self) -> tuple[int, int, int]:
+        r, w, f = C.c_uint32(), C.c_uint32(), C.c_uint32()
+        check(lib().gpu_serve_progress(C.byref(r), C.byref(w), C.byref(f)), "gpu_serve_progress")
+        return r.value, w.value, f.value
+
+    def poll(self, rid: int) -> dict:
+        st = GpuServeStatus()
+        check(lib().gpu_serve_poll(rid, C.byref(st)), "gpu_serve_poll")
+        return dict(state=SERVE_STATES[st.state], error=st.error, steps_completed=st.steps_completed,
+                    substeps=st.substeps, courant=st.courant, admit_s=st.admit_s, latency_s=st.latency_s)
+
+    def cancel(self, rid: int) -> None:
+        check(lib().gpu_serve_cancel(rid), "gpu_serve_cancel")
+
+    def result(self, rid: int) -> tuple[np.ndarray, np.ndarray, np.ndarray]:
+        n, cells = self._species[rid]
+        y, steps, failed = np.zeros((n, cells)), np.zeros(cells), np.zeros(cells)
+        check(lib().gpu_serve_result(rid, _p(y), _p(steps), _p(failed)), "gpu_serve_result")
+        return y, steps, failed
+
+    def forget(self, rid: int) -> None:
+        check(lib().gpu_serve_forget(rid), "gpu_serve_forget")
+        self._species.pop(rid, None)
+
+    def stats(self) -> dict:
+        st = GpuServeStats()
+        check(lib().gpu_serve_stats(C.byref(st)), "gpu_serve_stats")
+        return {name: getattr(st, name) for name, _ in GpuServeStats._fields_ if name != "reserved"}
+
+    def drain(self, timeout_s: float = 600.0, sleep_s: float = 2e-4) -> None:
+        """Drives the engine until nothing is running or waiting."""
+        import time
+        t_end = time.monotonic() + timeout_s
+        while True:
+            running, waiting, _ = self.progress()
+            if running == 0 and waiting == 0:
+                return
+            if time.monotonic() > t_end:
+                raise TimeoutError(f"serving: {running} running, {waiting} waiting after {timeout_s} s")
+            time.sleep(sleep_s)
+
+    def close(self) -> None:
+        check(lib().gpu_serve_close(), "gpu_serve_close")
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

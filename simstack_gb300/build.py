@@ -75,6 +75,7 @@ def build(force: bool = False, jobs: int | None = None) -> str:
         ("kern_probe.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "kern_probe.cu")]),
         ("gpu_module.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "gpu_module.cu")]),
         ("static_scratch.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "static_scratch.cu")]),
+        ("serve.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "serve.cu")]),
         ("mech.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "mech.cpp")]),
         ("host_api.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "host_api.cpp")]),
     ]

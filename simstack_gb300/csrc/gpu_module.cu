@@ -12,6 +12,7 @@
 #include "kin_kernels.cuh"
 #include "kin_table.cuh"
 #include "mech.h"
+#include "mech_tables.h"
 
 namespace sgb {
 cudaError_t launch_air_p0(const Shape &, const DevArgs &, cudaStream_t);
@@ -58,13 +59,6 @@ struct Module {
 Module g;
 
 const GpuKinTuning kDefaultTuning = {2u, 128u, 0u, 0u, 0.0f};   // CTA-synchronous queue, 128 threads, 255 registers
-
-bool is_rodas3(const KinMethod *m) {
-    KinMethod r = method_coefficients(2);
-    return m->stages == r.stages && m->order == r.order && memcmp(m->a, r.a, sizeof(r.a)) == 0 &&
-           memcmp(m->c, r.c, sizeof(r.c)) == 0 && memcmp(m->m, r.m, sizeof(r.m)) == 0 &&
-           memcmp(m->e, r.e, sizeof(r.e)) == 0 && m->gamma0 == r.gamma0 && memcmp(m->new_f, r.new_f, sizeof(r.new_f)) == 0;
-}
 
 void fill_args(const GpuKinLaunch *L, DevArgs *A) {
     memset(A, 0, sizeof(*A));
@@ -300,58 +294,17 @@ SGB_API int32_t gpu_step_points(float *x, float *y, float *z, float *vx, float *
 SGB_API int32_t gpu_kin_set_mech(const KinMech *mech, const KinMethod *method, const KinControl *control) {
     if (!g.ready) return (int32_t)cudaErrorInitializationError;
     if (!mech || !method || !control) return (int32_t)cudaErrorInvalidValue;
-    if (mech->species_count == 0 || mech->species_count > KIN_MAX_SPECIES || mech->reaction_count > KIN_MAX_REACTIONS ||
-        mech->nnz > KIN_MAX_NNZ || mech->lu_div_count > KIN_MAX_LU_DIV || mech->lu_sub_count > KIN_MAX_LU_SUB ||
-        method->stages < 2 || method->stages > KIN_MAX_STAGES)
-        return (int32_t)cudaErrorInvalidValue;
     // every table index must stay inside the tables (the kernels do not re-check)
-    const uint32_t n = mech->species_count, nnz = mech->nnz;
-    if (mech->div_begin[n] != mech->lu_div_count || mech->lower_begin[n] > KIN_MAX_NNZ || mech->upper_begin[n] > KIN_MAX_NNZ)
-        return (int32_t)cudaErrorInvalidValue;
-    for (uint32_t i = 0; i < n; ++i)
-        if (mech->diag[i] >= nnz || mech->div_begin[i] > mech->div_begin[i + 1] || mech->lower_begin[i] > mech->lower_begin[i + 1] ||
-            mech->upper_begin[i] > mech->upper_begin[i + 1])
-            return (int32_t)cudaErrorInvalidValue;
-    for (uint32_t d = 0; d < mech->lu_div_count; ++d) {
-        const KinLuDiv &v = mech->lu_div[d];
-        if (v.ik >= nnz || v.kk >= nnz || v.sub_begin > v.sub_end || v.sub_end > mech->lu_sub_count) return (int32_t)cudaErrorInvalidValue;
-    }
-    for (uint32_t s = 0; s < mech->lu_sub_count; ++s)
-        if (mech->lu_sub[s].ij >= nnz || mech->lu_sub[s].kj >= nnz) return (int32_t)cudaErrorInvalidValue;
-    for (uint32_t e = 0; e < mech->lower_begin[n]; ++e)
-        if (mech->lower[e].index >= nnz || mech->lower[e].col >= n) return (int32_t)cudaErrorInvalidValue;
-    for (uint32_t e = 0; e < mech->upper_begin[n]; ++e)
-        if (mech->upper[e].index >= nnz || mech->upper[e].col >= n) return (int32_t)cudaErrorInvalidValue;
-    for (uint32_t r = 0; r < mech->reaction_count; ++r) {
-        const KinReaction &rx = mech->reactions[r];
-        if (rx.reactant_count > KIN_MAX_REACTANTS || rx.net_count > KIN_MAX_NET) return (int32_t)cudaErrorInvalidValue;
-        for (uint32_t p = 0; p < rx.reactant_count; ++p) {
-            if (rx.reactant[p] >= n) return (int32_t)cudaErrorInvalidValue;
-            for (uint32_t e = 0; e < rx.net_count; ++e)
-                if (rx.jac_index[p][e] >= nnz) return (int32_t)cudaErrorInvalidValue;
-        }
-        for (uint32_t e = 0; e < rx.net_count; ++e)
-            if (rx.net_species[e] >= n) return (int32_t)cudaErrorInvalidValue;
-    }
-    // staged image: the record, then the Jacobian-pattern bitmask (slots some
-    // reaction scatters into, plus the diagonal)
-    static uint8_t image[kTableBytes];
-    memset(image, 0, sizeof(image));
-    memcpy(image, mech, sizeof(KinMech));
-    uint8_t *mask = image + kJacMaskOffset;
-    for (uint32_t i = 0; i < n; ++i) mask[mech->diag[i] >> 3] |= (uint8_t)(1u << (mech->diag[i] & 7));
-    for (uint32_t r = 0; r < mech->reaction_count; ++r) {
-        const KinReaction &rx = mech->reactions[r];
-        for (uint32_t p = 0; p < rx.reactant_count; ++p)
-            for (uint32_t e = 0; e < rx.net_count; ++e) mask[rx.jac_index[p][e] >> 3] |= (uint8_t)(1u << (rx.jac_index[p][e] & 7));
-    }
+    if (!mech_tables_valid(mech, method)) return (int32_t)cudaErrorInvalidValue;
+    static unsigned char image[kTableBytes];
+    table_image(mech, image);
     cudaError_t e = cudaMemcpyAsync(g.d_tables, image, kTableBytes, cudaMemcpyHostToDevice, g.stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
     if (e != cudaSuccess) return (int32_t)e;
     g.mech = *mech;
     g.method = *method;
     g.control = *control;
-    g.generated = fnv1a(mech, sizeof(KinMech)) == air_ops_signature() && is_rodas3(method);
+    g.generated = fnv1a(mech, sizeof(KinMech)) == air_ops_signature() && method_is_rodas3(method);
     g.have_mech = true;
     return 0;
 }
