@@ -244,6 +244,26 @@ SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *me
                                         const GpuKinLaunch *launch, void *stream, int32_t wait);
 
 /* ---------------------------------------------------------------------------
+ * Large mechanisms (new capability; the reference's u16 KinMech tables stop
+ * at 65,535 LU updates, and a 200-species / 1,200-reaction mechanism needs
+ * ~1.8 M). The cooperative kernels take a finalized host model (kin_model_*
+ * below) of up to 256 species and integrate one cell per CTA, every thread of
+ * the CTA sharing the cell's RHS, Jacobian, elimination and solves.
+ * precision 0: FP64, the same bits as the reference's solver on any mechanism
+ * (each LU element gets the reference's IKJ updates in the same order);
+ * precision 2: mixed (FP32 LU and solves in shared memory, FP64 RHS, Jacobian,
+ * residual refinement, state and control). The launch is a GpuKinLaunch over
+ * a zone block with the model's n and R rows; the work runs on the module
+ * stream (gpu_init first) and is waited for. */
+typedef struct KinModelHandle KinModelHandle;
+SGB_API int32_t gpu_kin_coop_set_mech(const KinModelHandle *model, const KinMethod *method, const KinControl *control);
+SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *launch, float *kernel_ms);
+/* out[8]: n, R, LU non-zeros, Jacobian entries, L entries, U entries, LU updates, image bytes. */
+SGB_API int32_t gpu_kin_coop_info(uint64_t *out);
+/* Refinement sweeps per stage solve of the mixed cooperative path (1..4, default 1). */
+SGB_API int32_t gpu_kin_coop_set_refinement(uint32_t sweeps);
+
+/* ---------------------------------------------------------------------------
  * Film advection and the served coupling step (new capability; the reference
  * has no GPU transport and no serving).
  *
@@ -325,7 +345,6 @@ SGB_API int32_t gpu_serve_close(void);
  * pattern, pivot order and bytes as kin_mech_finalize), rate constants and
  * the discharge source. A handle is an opaque model.
  */
-typedef struct KinModelHandle KinModelHandle;
 /* Rate-law kinds and parameters (kin_build.cpp:137-174):
  *   0 Arrhenius  p = {A, n, E}           k = A (T/300)^n exp(-E/T)
  *   1 third body p = {A, n, E}           same times [M]

@@ -160,6 +160,10 @@ def lib() -> C.CDLL:
             "gpu_copy_on_device": (i32, [vp, vp, u64]),
             "gpu_kin_advance_noalloc": (i32, [C.POINTER(KinMech), C.POINTER(KinMethod), C.POINTER(KinControl),
                                               C.POINTER(GpuKinLaunch), vp, i32]),
+            "gpu_kin_coop_set_mech": (i32, [vp, C.POINTER(KinMethod), C.POINTER(KinControl)]),
+            "gpu_kin_coop_advance": (i32, [C.POINTER(GpuKinLaunch), C.POINTER(f)]),
+            "gpu_kin_coop_info": (i32, [C.POINTER(u64)]),
+            "gpu_kin_coop_set_refinement": (i32, [u32]),
             "gpu_advect": (i32, [vp, u32, u32, u32, u32, vp, d, u32, vp]),
             "gpu_serve_open": (i32, [u64, C.POINTER(KinControl)]),
             "gpu_serve_set_mech": (i32, [C.POINTER(KinMech), C.POINTER(KinMethod)]),
@@ -500,6 +504,31 @@ class Module:
         solver-written prefix (src/sim/dbd.cpp:272-295). Returns kernel ms."""
         base = self.upload(z, device_base)
         ms = self.advance(z.launch(base, precision, duration), queue)
+        self.download(z, base)
+        return ms
+
+    # cooperative kernels (one CTA per cell): mechanisms beyond the KinMech tables
+    def coop_set_mech(self, model: "Model", meth: KinMethod | None = None, ctl: KinControl | None = None) -> None:
+        meth = meth if meth is not None else method("rodas3")
+        ctl = ctl if ctl is not None else control()
+        self._coop_keep = (model, meth, ctl)
+        check(lib().gpu_kin_coop_set_mech(model.h, C.byref(meth), C.byref(ctl)), "gpu_kin_coop_set_mech")
+
+    def coop_info(self) -> dict:
+        out = (C.c_uint64 * 8)()
+        check(lib().gpu_kin_coop_info(out), "gpu_kin_coop_info")
+        return dict(zip(("n", "R", "nnz", "jac_entries", "l_entries", "u_entries", "lu_updates", "image_bytes"),
+                        [int(v) for v in out]))
+
+    def coop_advance(self, L: GpuKinLaunch) -> float:
+        ms = C.c_float()
+        check(lib().gpu_kin_coop_advance(C.byref(L), C.byref(ms)), "gpu_kin_coop_advance")
+        return ms.value
+
+    def coop_integrate(self, z: ZoneBlock, duration: float, precision: int = 0, lane_count: int = 0,
+                       device_base: int | None = None) -> float:
+        base = self.upload(z, device_base)
+        ms = self.coop_advance(z.launch(base, precision, duration, lane_count))
         self.download(z, base)
         return ms
 

@@ -76,6 +76,8 @@ def build(force: bool = False, jobs: int | None = None) -> str:
         ("gpu_module.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "gpu_module.cu")]),
         ("static_scratch.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "static_scratch.cu")]),
         ("serve.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "serve.cu")]),
+        ("kern_coop.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "kern_coop.cu")]),
+        ("coop_build.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "coop_build.cpp")]),
         ("mech.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "mech.cpp")]),
         ("host_api.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "host_api.cpp")]),
     ]

@@ -20,6 +20,10 @@ struct KinModelHandle {
     Model model;
 };
 
+namespace sgb {
+const Model *model_of(const KinModelHandle *h) { return h ? &h->model : nullptr; }
+}   // namespace sgb
+
 SGB_API KinModelHandle *kin_model_new(void) { return new (std::nothrow) KinModelHandle(); }
 
 SGB_API KinModelHandle *kin_model_air(void) {

@@ -1,0 +1,636 @@
+// Cooperative kernels for large mechanisms: one CTA integrates one cell at a
+// time (persistent CTAs take cells from a work queue), its threads splitting
+// every phase of the Rosenbrock step -- rates per reaction, RHS per species,
+// Jacobian per entry, elimination per (row, column) of each pivot, solves per
+// row of each column. The step control is the reference's
+// (src/sim/kinetics/kin_solver.h:189-345): every thread runs the scalar
+// controller on the same values, so its decisions are uniform across the CTA.
+//
+// Precision 0: FP64 throughout, the same bits as the reference's solver (each
+// element sees the reference's operations in the reference's order; see
+// coop.h). The dense LU lives in per-CTA global scratch (L2-resident), with a
+// transposed copy of the factors for coalesced column reads in the solves.
+// Precision 2 (mixed): FP64 RHS, Jacobian, residual, state and control; the
+// LU and the triangular solves in FP32 with the dense LU in shared memory;
+// each stage solve refined with FP64 residual sweeps.
+
+#include <cuda_runtime.h>
+#include <string.h>
+
+#include <vector>
+
+#include "../../include/simstack_gpu.h"
+#include "coop.h"
+#include "kin_device.cuh"
+#include "mech.h"
+
+namespace sgb {
+
+namespace {
+
+constexpr uint32_t kCoopMaxSpecies = 256;   // register cache of a pivot row: 8 columns per lane
+constexpr uint32_t kCoopMaxCols = kCoopMaxSpecies / 32;
+
+struct CoopTab {
+    const CoopMech *h;
+    const uint16_t *reac;
+    const uint32_t *fbeg, *jbeg, *jpos, *jrow, *lbeg, *ubeg, *cbeg;
+    const CoopTerm *fent, *jent;
+    const uint16_t *jcol, *lrow, *ucol, *crow;
+
+    __device__ __forceinline__ void init(const void *image) {
+        const unsigned char *b = (const unsigned char *)image;
+        h = (const CoopMech *)b;
+        reac = (const uint16_t *)(b + h->off_reac);
+        fbeg = (const uint32_t *)(b + h->off_fbeg);
+        fent = (const CoopTerm *)(b + h->off_fent);
+        jbeg = (const uint32_t *)(b + h->off_jbeg);
+        jent = (const CoopTerm *)(b + h->off_jent);
+        jpos = (const uint32_t *)(b + h->off_jpos);
+        jrow = (const uint32_t *)(b + h->off_jrow);
+        jcol = (const uint16_t *)(b + h->off_jcol);
+        lbeg = (const uint32_t *)(b + h->off_lbeg);
+        lrow = (const uint16_t *)(b + h->off_lrow);
+        ubeg = (const uint32_t *)(b + h->off_ubeg);
+        ucol = (const uint16_t *)(b + h->off_ucol);
+        cbeg = (const uint32_t *)(b + h->off_cbeg);
+        crow = (const uint16_t *)(b + h->off_crow);
+    }
+};
+
+// Shared-memory doubles before the mixed path's FP32 arrays.
+__host__ __device__ inline uint32_t coop_smem_doubles(uint32_t n, uint32_t R) { return 11u * n + 2u * R + 8u; }
+
+template <int PREC>
+struct CoopCell {
+    typedef typename Pick<PREC == 0, double, float>::type Cf;   // LU and solve arithmetic
+    static constexpr bool kMixed = PREC == 2;
+    typedef RuntimeCoef M;
+
+    CoopTab tb;
+    uint32_t n, R, ld, nj, tid, NT, lane, warp, W;
+    double *y, *ytmp, *fcn, *src, *qv, *rb, *xv, *K, *kr, *rate, *red;
+    float *x32;
+    Cf *a;          // dense LU [n][ld]
+    Cf *tr;         // FP64: transposed factors [n][ld] (column k of L and U at row k)
+    double *js;     // mixed: Jacobian entries (a = -J) in FP64
+    // replicated scalar state (kin_solver.h:189-345)
+    double t, h, seg_end, applied, duration, period, first, count, steps, rejects, pulses, failed;
+    uint32_t iterations, transitions;
+    int phase;
+    bool pending, reject_last, reject_more;
+
+    __device__ __forceinline__ void sync() const { __syncthreads(); }
+
+    __device__ void load(const DevArgs &A, uint32_t cell) {
+        const uint32_t p = A.padded;
+        for (uint32_t s = tid; s < n; s += NT) {
+            y[s] = A.y[(size_t)s * p + cell];
+            src[s] = A.src[(size_t)s * p + cell];
+        }
+        for (uint32_t r = tid; r < R; r += NT) kr[r] = A.k[(size_t)r * p + cell];
+        h = A.h[cell];
+        period = A.period[cell];
+        first = A.pulse_first[cell];
+        count = A.pulse_count[cell];
+        duration = A.duration;
+        steps = rejects = pulses = 0.0;
+        failed = A.failed[cell];
+        t = 0.0;
+        applied = 0.0;
+        transitions = 0;
+        phase = kPhaseSegStart;
+        sync();
+    }
+
+    __device__ void store(const DevArgs &A, uint32_t cell) {
+        const uint32_t p = A.padded;
+        for (uint32_t s = tid; s < n; s += NT) A.y[(size_t)s * p + cell] = y[s];
+        if (tid == 0) {
+            A.h[cell] = h;
+            A.failed[cell] = failed;
+            A.steps[cell] += steps;
+            A.rejects[cell] += rejects;
+            A.pulses[cell] += pulses;
+        }
+        sync();
+    }
+
+    __device__ void seg_start(const DevArgs &A) {
+        pending = applied < count;
+        double next_pulse = sgb_fma(applied, period, first);
+        seg_end = pending ? vmin(next_pulse, duration) : duration;
+        bool active = t < seg_end && !(failed > 0.0);
+        reject_last = false;
+        reject_more = false;
+        h = h > 0.0 ? h : A.ctl.h_start;
+        iterations = 0;
+        phase = active ? kPhaseStepping : kPhaseSegFinish;
+    }
+
+    __device__ void seg_finish(const DevArgs &A, uint32_t cell) {
+        bool alive = !(failed > 0.0);
+        bool hit = pending && alive && t >= seg_end;
+        if (hit) {
+            const uint32_t p = A.padded;
+            for (uint32_t s = tid; s < n; s += NT) y[s] = y[s] + A.pulse[(size_t)s * p + cell];
+            sync();
+            applied = applied + 1.0;
+            pulses = pulses + 1.0;
+            h = A.ctl.h_start;
+        }
+        bool done = (t >= duration && applied >= count) || !alive;
+        phase = done ? kPhaseDone : kPhaseSegStart;
+    }
+
+    // As the lane kernels' settle: transitions until a step attempt is due (true) or the cell is done.
+    __device__ bool settle(const DevArgs &A, uint32_t cell) {
+        for (;;) {
+            if (++transitions > (1u << 24)) {
+                failed = 1.0;
+                phase = kPhaseDone;
+            }
+            switch (phase) {
+                case kPhaseSegStart: seg_start(A); break;
+                case kPhaseSegFinish: seg_finish(A, cell); break;
+                case kPhaseStepping:
+                    if (++iterations > A.ctl.max_steps) {
+                        failed = 1.0;
+                        phase = kPhaseSegFinish;
+                        break;
+                    }
+                    return true;
+                default: return false;
+            }
+        }
+    }
+
+    // fcn = f(yy): rates per reaction, then each species' terms in reaction order.
+    __device__ void rhs(const double *yy) {
+        for (uint32_t r = tid; r < R; r += NT) {
+            const uint16_t *rc = tb.reac + (size_t)r * 4;
+            double v = kr[r];
+            for (uint32_t p = 0; p < rc[0]; ++p) v = v * yy[rc[1 + p]];
+            rate[r] = v;
+        }
+        sync();
+        for (uint32_t s = tid; s < n; s += NT) {
+            double f = src[s];
+            for (uint32_t e = tb.fbeg[s]; e < tb.fbeg[s + 1]; ++e) {
+                const CoopTerm term = tb.fent[e];
+                f = sgb_fma((double)term.coef, rate[term.index], f);
+            }
+            fcn[s] = f;
+        }
+        sync();
+    }
+
+    // a = -J at yy (zero elsewhere); mixed: the FP64 entries also kept in js.
+    __device__ void neg_jac(const double *yy) {
+        const uint32_t total = n * ld;
+        for (uint32_t q = tid; q < total; q += NT) a[q] = (Cf)0.0;
+        sync();
+        for (uint32_t e = tid; e < nj; e += NT) {
+            double acc = 0.0;
+            for (uint32_t q = tb.jbeg[e]; q < tb.jbeg[e + 1]; ++q) {
+                const CoopTerm term = tb.jent[q];
+                const uint32_t r = term.index & 0xffffffu, p = term.index >> 24;
+                const uint16_t *rc = tb.reac + (size_t)r * 4;
+                double d = kr[r];
+                for (uint32_t o = 0; o < rc[0]; ++o)
+                    if (o != p) d = d * yy[rc[1 + o]];
+                acc = sgb_fma((double)term.coef, d, acc);
+            }
+            if constexpr (kMixed) js[e] = acc;
+            a[tb.jpos[e]] = (Cf)acc;
+        }
+        sync();
+    }
+
+    // In place: a -> L\U of (I ghinv - J), diagonal holding 1/U(k,k); pivot by
+    // pivot (kin_solver.h:97-113 applies the same updates row by row).
+    __device__ void factor(Cf ghinv) {
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t lb = tb.lbeg[k], nl = tb.lbeg[k + 1] - lb;
+            const uint32_t ub = tb.ubeg[k], nu = tb.ubeg[k + 1] - ub;
+            const Cf inv = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
+            // L column k: l_i = a[i][k] / U(k,k)
+            for (uint32_t li = tid; li < nl; li += NT) {
+                const uint32_t i = tb.lrow[lb + li];
+                const Cf l = a[(size_t)i * ld + k] * inv;
+                a[(size_t)i * ld + k] = l;
+                if constexpr (!kMixed) tr[(size_t)k * ld + i] = l;
+            }
+            if (nl) sync();
+            if (tid == 0) {
+                a[(size_t)k * ld + k] = inv;
+                if constexpr (!kMixed) tr[(size_t)k * ld + k] = inv;
+            }
+            // pivot row k (final) cached per lane; rows of L(k) updated warp by warp
+            Cf pv[kCoopMaxCols];
+            uint32_t cj[kCoopMaxCols];
+#pragma unroll
+            for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
+                const uint32_t uj = lane + 32u * c;
+                cj[c] = uj < nu ? tb.ucol[ub + uj] : 0u;
+                pv[c] = uj < nu ? a[(size_t)k * ld + cj[c]] : (Cf)0.0;
+            }
+            if constexpr (!kMixed) {
+                if (warp == 0) {
+#pragma unroll
+                    for (uint32_t c = 0; c < kCoopMaxCols; ++c)
+                        if (lane + 32u * c < nu) tr[(size_t)cj[c] * ld + k] = pv[c];
+                }
+            }
+            if (nl == 0) continue;   // nothing below the pivot: the next pivot reads none of this pivot's writes
+            for (uint32_t li = warp; li < nl; li += W) {
+                const uint32_t i = tb.lrow[lb + li];
+                Cf *row = a + (size_t)i * ld;
+                const Cf l = row[k];
+#pragma unroll
+                for (uint32_t c = 0; c < kCoopMaxCols; ++c)
+                    if (lane + 32u * c < nu) row[cj[c]] = sgb_fma(-l, pv[c], row[cj[c]]);
+            }
+            sync();
+        }
+        sync();
+    }
+
+    // x = (LU)^-1 x in place, column-oriented (the reference's row order per element);
+    // out receives the result (it may alias nothing else).
+    template <class V>
+    __device__ void solve(V *x, V *out) {
+        const Cf *f = kMixed ? a : tr;   // mixed: columns of a (odd stride: conflict-free); FP64: rows of tr
+        for (uint32_t k = 0; k < n; ++k) {
+            const uint32_t lb = tb.lbeg[k], nl = tb.lbeg[k + 1] - lb;
+            if (nl == 0) continue;
+            const V xk = x[k];
+            for (uint32_t li = tid; li < nl; li += NT) {
+                const uint32_t i = tb.lrow[lb + li];
+                const V lik = kMixed ? (V)f[(size_t)i * ld + k] : (V)f[(size_t)k * ld + i];
+                x[i] = sgb_fma(-lik, xk, x[i]);
+            }
+            sync();
+        }
+        for (uint32_t k = n; k-- > 0;) {
+            const V xk = x[k] * (V)f[(size_t)k * ld + k];
+            if (tid == 0) out[k] = xk;
+            const uint32_t cb = tb.cbeg[k], nc = tb.cbeg[k + 1] - cb;
+            if (nc == 0) continue;
+            for (uint32_t ci = tid; ci < nc; ci += NT) {
+                const uint32_t i = tb.crow[cb + ci];
+                const V uik = kMixed ? (V)f[(size_t)i * ld + k] : (V)f[(size_t)k * ld + i];
+                x[i] = sgb_fma(-uik, xk, x[i]);
+            }
+            sync();
+        }
+        sync();
+    }
+
+    // Mixed: out = W^-1 rb by the FP32 LU, then `sweeps` FP64-residual refinement sweeps.
+    __device__ void solve_refined(const DevArgs &A, double ghinv, double *out) {
+        float *xs = x32, *xo = x32 + kCoopMaxSpecies;
+        for (uint32_t s = tid; s < n; s += NT) xs[s] = (float)rb[s];
+        sync();
+        solve(xs, xo);
+        for (uint32_t s = tid; s < n; s += NT) out[s] = (double)xo[s];
+        sync();
+        for (uint32_t sw = 0; sw < A.ir_sweeps; ++sw) {
+            for (uint32_t i = tid; i < n; i += NT) {
+                double w = ghinv * out[i];
+                for (uint32_t e = tb.jrow[i]; e < tb.jrow[i + 1]; ++e) w = sgb_fma(js[e], out[tb.jcol[e]], w);
+                xs[i] = (float)(rb[i] - w);
+            }
+            sync();
+            solve(xs, xo);
+            for (uint32_t s = tid; s < n; s += NT) out[s] = out[s] + (double)xo[s];
+            sync();
+        }
+    }
+
+    // One pass of kin_integrate's step loop (kin_solver.h:216-311).
+    __device__ void attempt(const DevArgs &A) {
+        const double h_min = A.ctl.h_min, rtol = A.ctl.rtol, atol = A.ctl.atol;
+        const double inv_n = 1.0 / (double)n;
+        double remaining = seg_end - t;
+        double h_cap = remaining;
+        if (A.ctl.h_max > 0.0) h_cap = vmin(h_cap, A.ctl.h_max);
+        double h_wanted = vmax(h, h_min);
+        bool last = h_wanted >= remaining;
+        double hs = last ? remaining : vmin(h_wanted, h_cap);
+
+        rhs(y);
+        neg_jac(y);
+        const double ghinv = 1.0 / (hs * M::gamma0(A));
+        factor((Cf)ghinv);
+        const double hinv = 1.0 / hs;
+
+        bool fcn_at_y = true;
+        const int S = M::stages(A);
+        for (int st = 0; st < S; ++st) {
+            const int packed = st * (st - 1) / 2;
+            double *Ks = K + (size_t)st * n;
+            if (st > 0 && M::new_f(A, st)) {
+                bool moved = false;
+                for (int j = 0; j < st; ++j)
+                    if (M::a(A, packed + j) != 0.0) moved = true;
+                if (moved || !fcn_at_y) {
+                    for (uint32_t s = tid; s < n; s += NT) {
+                        double v = y[s];
+                        for (int j = 0; j < st; ++j) {
+                            const double av = M::a(A, packed + j);
+                            if (av == 0.0) continue;
+                            v = sgb_fma(av, K[(size_t)j * n + s], v);
+                        }
+                        ytmp[s] = v;
+                    }
+                    sync();
+                    rhs(ytmp);
+                    fcn_at_y = !moved;
+                }
+            }
+            for (uint32_t s = tid; s < n; s += NT) {
+                double v = fcn[s];
+                for (int j = 0; j < st; ++j) {
+                    const double c = M::c(A, packed + j);
+                    if (c == 0.0) continue;
+                    v = sgb_fma(c * hinv, K[(size_t)j * n + s], v);
+                }
+                if constexpr (kMixed) rb[s] = v;
+                else Ks[s] = v;
+            }
+            sync();
+            if constexpr (kMixed) {
+                solve_refined(A, ghinv, Ks);
+            } else {
+                solve(Ks, xv);
+                for (uint32_t s = tid; s < n; s += NT) Ks[s] = xv[s];
+                sync();
+            }
+        }
+
+        // y_new into ytmp and the weighted RMS error (kin_solver.h:263-280)
+        for (uint32_t s = tid; s < n; s += NT) {
+            double ynew = y[s], yerr = 0.0;
+            for (int st = 0; st < S; ++st) {
+                const double mc = M::m(A, st), ec = M::e(A, st);
+                if (mc != 0.0) ynew = sgb_fma(mc, K[(size_t)st * n + s], ynew);
+                if (ec != 0.0) yerr = sgb_fma(ec, K[(size_t)st * n + s], yerr);
+            }
+            const double scale = sgb_fma(rtol, vmax(vabs(y[s]), vabs(ynew)), atol);
+            qv[s] = yerr / scale;
+            ytmp[s] = ynew;
+        }
+        sync();
+        if (tid == 0) {
+            double e = 0.0;
+            for (uint32_t s = 0; s < n; ++s) e = sgb_fma(qv[s], qv[s], e);
+            red[0] = e;
+        }
+        sync();
+        double err = vsqrt(red[0] * inv_n);
+        if (!is_finite_lane(err)) err = 1e10;
+
+        double fac = step_factor(err, M::order(A));
+        bool ok = err <= 1.0 || hs <= h_min;
+        if (A.ctl.fixed_step) {
+            ok = true;
+            fac = 1.0;
+        }
+        if (ok) {
+            for (uint32_t s = tid; s < n; s += NT) {
+                double ynew = ytmp[s];
+                if (A.ctl.clamp_negative) ynew = vmax(ynew, 0.0);
+                y[s] = ynew;
+            }
+            t = last ? seg_end : t + hs;
+        }
+        double h_acc = hs * fac;
+        h_acc = reject_last ? vmin(h_acc, hs) : h_acc;
+        h_acc = (last && fac >= 1.0) ? vmax(h_acc, h_wanted) : h_acc;
+        double h_rej = reject_more ? hs * 0.1 : vmin(hs * fac, hs);
+        if (A.ctl.fixed_step) {
+            h_acc = h_wanted;
+            h_rej = h_wanted;
+        }
+        h = ok ? h_acc : h_rej;
+        reject_more = !ok && reject_last;
+        reject_last = !ok;
+        steps = steps + (ok ? 1.0 : 0.0);
+        rejects = rejects + (ok ? 0.0 : 1.0);
+        if (!(t < seg_end && !(failed > 0.0))) phase = kPhaseSegFinish;
+        sync();
+    }
+};
+
+template <int PREC>
+__global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant__ DevArgs A, double *scratch, uint64_t stride) {
+    extern __shared__ __align__(16) double sm[];
+    __shared__ uint32_t cell_s;
+    CoopCell<PREC> C;
+    C.tb.init(A.tables);
+    C.n = C.tb.h->n;
+    C.R = C.tb.h->R;
+    C.ld = C.tb.h->ld;
+    C.nj = C.tb.h->nj;
+    C.tid = threadIdx.x;
+    C.NT = blockDim.x;
+    C.lane = threadIdx.x & 31u;
+    C.warp = threadIdx.x >> 5;
+    C.W = blockDim.x >> 5;
+    const uint32_t n = C.n;
+    C.y = sm;
+    C.ytmp = C.y + n;
+    C.fcn = C.ytmp + n;
+    C.src = C.fcn + n;
+    C.qv = C.src + n;
+    C.rb = C.qv + n;
+    C.xv = C.rb + n;
+    C.K = C.xv + n;   // 4 stage vectors
+    C.kr = C.K + 4 * n;
+    C.rate = C.kr + C.R;
+    C.red = C.rate + C.R;
+    C.x32 = (float *)(sm + coop_smem_doubles(n, C.R));
+    double *g = scratch + (size_t)blockIdx.x * stride;
+    if constexpr (PREC == 2) {
+        C.a = (typename CoopCell<PREC>::Cf *)(C.x32 + 2 * kCoopMaxSpecies);
+        C.tr = nullptr;
+        C.js = g;
+    } else {
+        C.a = (typename CoopCell<PREC>::Cf *)g;
+        C.tr = (typename CoopCell<PREC>::Cf *)(g + (size_t)n * C.ld);
+        C.js = nullptr;
+    }
+    for (;;) {
+        if (threadIdx.x == 0) cell_s = atomicAdd(A.cursor, 1u);
+        __syncthreads();
+        const uint32_t cell = cell_s;
+        __syncthreads();
+        if (cell >= A.lanes) break;
+        C.load(A, cell);
+        while (C.settle(A, cell)) C.attempt(A);
+        C.store(A, cell);
+    }
+}
+
+// Module state of the cooperative path.
+struct CoopModule {
+    bool ready = false;
+    std::vector<uint8_t> image;
+    CoopMech head;
+    void *d_image = nullptr;
+    uint32_t *d_header = nullptr;   // cursor (+0), error flag (+32 words)
+    double *d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    KinMethod method;
+    KinControl control;
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    uint32_t ir_sweeps = 1;
+    float last_ms = 0.0f;
+};
+CoopModule cm;
+
+size_t coop_smem_bytes(int prec, const CoopMech &h) {
+    size_t b = (size_t)coop_smem_doubles(h.n, h.R) * 8;
+    if (prec == 2) b += 2 * kCoopMaxSpecies * 4 + (size_t)h.n * h.ld * 4;
+    return b;
+}
+
+size_t coop_scratch_doubles(int prec, const CoopMech &h) {
+    size_t d = prec == 2 ? (size_t)h.nj : 2 * (size_t)h.n * h.ld;
+    return (d + 31) / 32 * 32;   // 256-byte aligned per CTA
+}
+
+}   // namespace
+}   // namespace sgb
+
+using namespace sgb;
+
+namespace sgb {
+const Model *model_of(const KinModelHandle *h);
+}
+
+SGB_API int32_t gpu_kin_coop_set_mech(const KinModelHandle *model, const KinMethod *method, const KinControl *control) {
+    if (!model || !method || !control || method->stages < 2 || method->stages > 4) return (int32_t)cudaErrorInvalidValue;
+    const Model *m = model_of(model);
+    if (!m || !m->finalized || m->n() > kCoopMaxSpecies) return (int32_t)cudaErrorInvalidValue;
+    std::vector<uint8_t> img;
+    if (!coop_image(*m, &img)) return (int32_t)cudaErrorInvalidValue;
+    CoopMech h;
+    memcpy(&h, img.data(), sizeof(h));
+    int dev = 0, sms = 0, max_smem = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (coop_smem_bytes(0, h) > (size_t)max_smem) return (int32_t)cudaErrorInvalidValue;
+    if (cm.d_image) cudaFree(cm.d_image);
+    cm.d_image = nullptr;
+    if (!cm.d_header) {
+        e = cudaMalloc((void **)&cm.d_header, 256);
+        if (e != cudaSuccess) return (int32_t)e;
+    }
+    e = cudaMalloc(&cm.d_image, img.size());
+    if (e == cudaSuccess) e = cudaMemcpy(cm.d_image, img.data(), img.size(), cudaMemcpyHostToDevice);
+    // scratch for the larger of the two precisions' needs, one slot per resident CTA (one CTA per SM)
+    const size_t per = coop_scratch_doubles(0, h) > coop_scratch_doubles(2, h) ? coop_scratch_doubles(0, h)
+                                                                              : coop_scratch_doubles(2, h);
+    const size_t need = per * 8 * (size_t)sms;
+    if (e == cudaSuccess && need > cm.scratch_bytes) {
+        if (cm.d_scratch) cudaFree(cm.d_scratch);
+        cm.d_scratch = nullptr;
+        cm.scratch_bytes = 0;
+        e = cudaMalloc((void **)&cm.d_scratch, need);
+        if (e == cudaSuccess) cm.scratch_bytes = need;
+    }
+    if (e == cudaSuccess && !cm.ev0) e = cudaEventCreate(&cm.ev0);
+    if (e == cudaSuccess && !cm.ev1) e = cudaEventCreate(&cm.ev1);
+    if (e != cudaSuccess) return (int32_t)e;
+    cm.image.swap(img);
+    cm.head = h;
+    cm.method = *method;
+    cm.control = *control;
+    cm.ready = true;
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *L, float *kernel_ms) {
+    if (!cm.ready || !L) return (int32_t)cudaErrorInvalidValue;
+    if ((L->precision != 0 && L->precision != 2) || L->padded == 0 || L->lane_count > L->padded)
+        return (int32_t)cudaErrorInvalidValue;
+    if (!(L->duration >= 0.0) || L->duration > 1.0e300) return (int32_t)cudaErrorInvalidValue;
+    if (!L->y || !L->h || !L->steps || !L->rejects || !L->pulses || !L->failed || !L->k || !L->src || !L->pulse ||
+        !L->period || !L->pulse_first || !L->pulse_count)
+        return (int32_t)cudaErrorInvalidValue;
+    const int prec = (int)L->precision;
+    int max_smem = 0;
+    if (cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0) != cudaSuccess ||
+        coop_smem_bytes(prec, cm.head) > (size_t)max_smem)
+        return (int32_t)cudaErrorInvalidValue;   // the mixed path's FP32 LU must fit one CTA's shared memory
+    DevArgs A;
+    memset(&A, 0, sizeof(A));
+    A.y = L->y; A.h = L->h; A.steps = L->steps; A.rejects = L->rejects; A.pulses = L->pulses; A.failed = L->failed;
+    A.k = L->k; A.src = L->src; A.pulse = L->pulse; A.period = L->period;
+    A.pulse_first = L->pulse_first; A.pulse_count = L->pulse_count;
+    A.padded = L->padded;
+    A.lanes = L->lane_count ? L->lane_count : L->padded;
+    A.duration = L->duration;
+    A.ctl = cm.control;
+    memcpy(A.ma, cm.method.a, sizeof(A.ma));
+    memcpy(A.mc, cm.method.c, sizeof(A.mc));
+    memcpy(A.mm, cm.method.m, sizeof(A.mm));
+    memcpy(A.me, cm.method.e, sizeof(A.me));
+    A.gamma0 = cm.method.gamma0;
+    memcpy(A.new_f, cm.method.new_f, sizeof(A.new_f));
+    A.stages = cm.method.stages;
+    A.order = cm.method.order;
+    A.ir_sweeps = cm.ir_sweeps;
+    A.cursor = cm.d_header;
+    A.error_flag = cm.d_header + 32;
+    A.tables = cm.d_image;
+    A.table_bytes = cm.head.bytes;
+    if (A.lanes == 0 || A.duration == 0.0) {
+        if (kernel_ms) *kernel_ms = 0.0f;
+        return 0;
+    }
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return (int32_t)e;
+    void (*fn)(DevArgs, double *, uint64_t) = prec == 0 ? kin_coop_kernel<0> : kin_coop_kernel<2>;
+    const size_t smem = coop_smem_bytes(prec, cm.head);
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e != cudaSuccess) return (int32_t)e;
+    const uint32_t grid = (uint32_t)sms < A.lanes ? (uint32_t)sms : A.lanes;
+    const uint64_t stride = coop_scratch_doubles(prec, cm.head);
+    cudaStream_t s = (cudaStream_t)gpu_stream();
+    e = cudaMemsetAsync(cm.d_header, 0, 256, s);
+    if (e == cudaSuccess) e = cudaEventRecord(cm.ev0, s);
+    if (e != cudaSuccess) return (int32_t)e;
+    fn<<<grid, 512, smem, s>>>(A, cm.d_scratch, stride);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(cm.ev1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(cm.ev1);
+    if (e != cudaSuccess) return (int32_t)e;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, cm.ev0, cm.ev1);
+    cm.last_ms = ms;
+    if (kernel_ms) *kernel_ms = ms;
+    return 0;
+}
+
+// Counts of the cooperative path's mechanism image: n, R, nnz, Jacobian
+// entries, L entries, U entries, LU updates, image bytes.
+SGB_API int32_t gpu_kin_coop_info(uint64_t *out8) {
+    if (!cm.ready || !out8) return (int32_t)cudaErrorInvalidValue;
+    const CoopMech &h = cm.head;
+    out8[0] = h.n; out8[1] = h.R; out8[2] = h.nnz; out8[3] = h.nj;
+    out8[4] = h.l_entries; out8[5] = h.u_entries; out8[6] = h.lu_updates; out8[7] = h.bytes;
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_coop_set_refinement(uint32_t sweeps) {
+    if (sweeps < 1 || sweeps > 4) return (int32_t)cudaErrorInvalidValue;
+    cm.ir_sweeps = sweeps;
+    return 0;
+}
