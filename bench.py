@@ -184,6 +184,13 @@ def flops_per_step(model) -> dict:
     return {"fun": fun, "neg_jac": jac, "factor": lu, "solve": solve, "total": total}
 
 
+# DRAM bytes (read + write) per attempted cell-step of the queue kernels, from one ncu capture each
+# (262,144 cells x 0.5 s, `bench.py --profile-case f64|mixed`; summaries in
+# profiles/kin_queue_cta_{f64,mixed}_air_262144x0.5s.txt). Nearly all of it is local-memory spill
+# traffic, which grows with the cell-steps a launch executes; the bench scales it to its own launch.
+DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 8624.7}
+
+
 def hbm_bytes_per_cell(n: int, R: int) -> int:
     # read y, k, src, h, failed, period/first/count once; write y, h, steps, rejects, failed once
     return 8 * (2 * n + R + n + 6)
@@ -413,7 +420,10 @@ def run_ours(args):
         "steps_per_cell": {"mean": steps_total / cells, "failed_cells": failed},
         "roofline": {"bound": "fp64", "achieved": ach64 if head == "f64" else achmx, "peak": fp64_peak,
                      "unit": "TFLOP/s", "frac": (ach64 if head == "f64" else achmx) / fp64_peak,
-                     "traffic": None,
+                     "traffic": DRAM_BYTES_PER_CELL_STEP[head] * steps_total,
+                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per launch: the per-cell-step "
+                                     "figure of one ncu capture (262,144 cells x 0.5 s) x this launch's attempted "
+                                     "cell-steps (FP64-path counts); local-memory spills, not algorithmic bytes",
                      "peak_source": "FP64 FMA throughput measured in this run (gpu_probe_throughput kind 0), x2 flops",
                      "algorithmic_flops_per_step": flops["total"],
                      "note": "algorithmic flops = FP64 path step count (= the oracle's) x flops per Rodas3 step; "

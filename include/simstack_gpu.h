@@ -209,6 +209,12 @@ SGB_API int32_t gpu_kin_last_stats(uint64_t *kernel_launches, float *last_kernel
 
 /* Mixed path (precision 2): iterative-refinement sweeps per stage solve, 1 (default) or 2. */
 SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps);
+/* Mixed path (precision 2) variant: 0 = FP32 Jacobian / LU / solves with an FP64-residual refinement
+ * sweep per stage, FP64 state; 1 = double-float state (hi + lo FP32 pairs) with FP32 stage vectors,
+ * LU and solves, stage right-hand sides accumulated in double-float, almost no FP64 work per species
+ * (only the scalar step controller stays FP64). */
+SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant);
+SGB_API uint32_t gpu_kin_get_mixed_variant(void);
 
 /* Measured instruction throughput of this device, operations per second (an
  * FMA is one operation): kind 0 FP64 FMA, 1 FP32 FMA, 2 FP32->FP64->FP32

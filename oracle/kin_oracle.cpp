@@ -1045,6 +1045,160 @@ static void integrate_mixed(const Mechanism &m, const Method &me, const Control 
     }
 }
 
+// Model of the module's mixed path with DOUBLE-FLOAT STATE (mixed variant 1),
+// in the GPU kernel's operation order (LaneDf in the module): y and f(y) are
+// hi + lo FP32 pairs; -J, LU, stage vectors K and solves FP32; the stage
+// right-hand side f(y) [+ df] + sum_j (c_j / h) K_j accumulated in
+// double-float and rounded once; y_new = y + sum m K in double-float; the
+// error norm in FP32; only t and h stay FP64.
+static inline Df2 df_add_f(Df2 a, float b) {
+    float s = a.hi + b;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b - bb);
+    e = e + a.lo;
+    float t = s + e;
+    return Df2{t, e - (t - s)};
+}
+static inline Df2 df_prod_f(float a, float b) {
+    float p = a * b;
+    return Df2{p, std::fma(a, b, -p)};
+}
+
+static void integrate_mixed_df(const Mechanism &m, const Method &me, const Control &ctl, Df2 *y, double &t, double t_end,
+                               double &h, Stats<double> &st, MixedWork &w) {
+    const u32 n = m.n();
+    std::vector<float> yhi(n), d32(n), df32(n), nhi(n), nlo(n), kst((size_t)4 * n);
+    float *K[4] = {kst.data(), kst.data() + n, kst.data() + 2 * n, kst.data() + 3 * n};
+    float *a = w.a.data();
+    const float rtol = (float)ctl.rtol, atol = (float)ctl.atol, inv_n = 1.0f / (float)n;
+    bool active = t < t_end && !(st.failed > 0.0);
+    bool reject_last = false, reject_more = false;
+    h = h > 0.0 ? h : ctl.h_start;
+    u32 iterations = 0;
+    while (active) {
+        if (++iterations > ctl.max_steps) { st.failed = 1.0; break; }
+        double remaining = t_end - t;
+        double h_cap = remaining;
+        if (ctl.h_max > 0.0) h_cap = vmin(h_cap, ctl.h_max);
+        double h_wanted = vmax(h, ctl.h_min);
+        bool last = h_wanted >= remaining;
+        double hs = last ? remaining : vmin(h_wanted, h_cap);
+        const float hs32 = (float)hs;
+
+        eval_fun_df(m, w.kd.data(), w.sd.data(), y, w.fd.data());
+        for (u32 s = 0; s < n; ++s) yhi[s] = y[s].hi;
+        eval_neg_jac(m, w.k32.data(), yhi.data(), a);
+        factor(m, 1.0f / (hs32 * (float)me.gamma0), a);
+        const float hinv = 1.0f / hs32;
+
+        bool last_moved = false;
+        for (u32 stg = 0; stg < me.stages; ++stg) {
+            u32 packed = stg * (stg - 1) / 2;
+            if (stg > 0 && me.new_f[stg]) {
+                bool moved = false;
+                for (u32 s = 0; s < n; ++s) d32[s] = 0.0f;
+                for (u32 j = 0; j < stg; ++j) {
+                    float av = (float)me.a[packed + j];
+                    if (av == 0.0f) continue;
+                    moved = true;
+                    for (u32 s = 0; s < n; ++s) d32[s] = std::fma(av, K[j][s], d32[s]);
+                }
+                if (moved) eval_fun_delta32(m, w.k32.data(), yhi.data(), d32.data(), df32.data());
+                last_moved = moved;
+            }
+            for (u32 s = 0; s < n; ++s) {
+                Df2 b = w.fd[s];
+                if (last_moved) b = df_add_f(b, df32[s]);
+                for (u32 j = 0; j < stg; ++j) {
+                    float c = (float)me.c[packed + j];
+                    if (c == 0.0f) continue;
+                    b = df_add(b, df_prod_f(c * hinv, K[j][s]));
+                }
+                K[stg][s] = b.hi + b.lo;
+            }
+            solve(m, a, K[stg]);
+        }
+
+        float err = 0.0f;
+        for (u32 s = 0; s < n; ++s) {
+            Df2 yn = y[s];
+            float yerr = 0.0f;
+            for (u32 stg = 0; stg < me.stages; ++stg) {
+                float mc = (float)me.m[stg], ec = (float)me.e[stg];
+                if (mc != 0.0f) yn = df_add(yn, df_prod_f(mc, K[stg][s]));
+                if (ec != 0.0f) yerr = std::fma(ec, K[stg][s], yerr);
+            }
+            float scale = std::fma(rtol, std::fmax(std::fabs(y[s].hi), std::fabs(yn.hi)), atol);
+            float q = yerr / scale;
+            err = std::fma(q, q, err);
+            nhi[s] = yn.hi;
+            nlo[s] = yn.lo;
+        }
+        err = vsqrt(err * inv_n);
+        if (!finite(err)) err = 1e10f;
+        float fac32 = step_factor(err, me.order);
+        bool ok = err <= 1.0f || hs <= ctl.h_min;
+        if (ctl.fixed_step) { ok = true; fac32 = 1.0f; }
+        if (ok) {
+            for (u32 s = 0; s < n; ++s) {
+                float hi = nhi[s], lo = nlo[s];
+                if (ctl.clamp_negative && (hi < 0.0f || (hi == 0.0f && lo < 0.0f))) { hi = 0.0f; lo = 0.0f; }
+                y[s] = Df2{hi, lo};
+            }
+            t = last ? t_end : t + hs;
+        }
+        const double fac = (double)fac32;
+        double h_acc = hs * fac;
+        h_acc = reject_last ? vmin(h_acc, hs) : h_acc;
+        h_acc = (last && fac >= 1.0) ? vmax(h_acc, h_wanted) : h_acc;
+        double h_rej = reject_more ? hs * 0.1 : vmin(hs * fac, hs);
+        if (ctl.fixed_step) { h_acc = h_wanted; h_rej = h_wanted; }
+        h = ok ? h_acc : h_rej;
+        reject_more = !ok && reject_last;
+        reject_last = !ok;
+        st.steps = st.steps + (ok ? 1.0 : 0.0);
+        st.rejects = st.rejects + (ok ? 0.0 : 1.0);
+        active = t < t_end && !(st.failed > 0.0);
+    }
+}
+
+static void advance_mixed_df_lane(const Mechanism &m, const Method &me, const Control &ctl, const LaneArrays &a, u32 i,
+                                  double duration, MixedWork &w, std::vector<Df2> &y) {
+    const u32 n = m.n(), R = m.R(), p = a.padded;
+    for (u32 s = 0; s < n; ++s) {
+        y[s] = df_from(a.y[(size_t)s * p + i]);
+        w.sd[s] = df_from(a.src[(size_t)s * p + i]);
+    }
+    for (u32 r = 0; r < R; ++r) {
+        w.kd[r] = df_from(a.k[(size_t)r * p + i]);
+        w.k32[r] = w.kd[r].hi;
+    }
+    double h = a.h[i], per = a.period[i], first = a.pulse_first[i], count = a.pulse_count[i];
+    Stats<double> st = {0.0, 0.0, 0.0, a.failed[i]};
+    double t = 0.0, applied = 0.0;
+    for (;;) {
+        bool pending = applied < count;
+        double next_pulse = std::fma(applied, per, first);
+        double seg_end = pending ? vmin(next_pulse, duration) : duration;
+        integrate_mixed_df(m, me, ctl, y.data(), t, seg_end, h, st, w);
+        bool alive = !(st.failed > 0.0);
+        bool hit = pending && alive && t >= seg_end;
+        if (hit) {
+            for (u32 s = 0; s < n; ++s) y[s] = df_add(y[s], df_from(a.pulse[(size_t)s * p + i]));
+            applied = applied + 1.0;
+            st.pulses = st.pulses + 1.0;
+            h = ctl.h_start;
+        }
+        if ((t >= duration && applied >= count) || !alive) break;
+    }
+    for (u32 s = 0; s < n; ++s) a.y[(size_t)s * p + i] = df_to(y[s]);
+    a.h[i] = h;
+    a.failed[i] = st.failed;
+    a.steps[i] += st.steps;
+    a.rejects[i] += st.rejects;
+    a.pulses[i] += st.pulses;
+}
+
 // kin_advance for the mixed model: segments between pulses, as advance() above.
 static void advance_mixed_lane(const Mechanism &m, const Method &me, const Control &ctl, u32 sweeps, const LaneArrays &a,
                                u32 i, double duration, MixedWork &w, std::vector<double> &y) {
@@ -1083,12 +1237,16 @@ static void advance_mixed_lane(const Mechanism &m, const Method &me, const Contr
     a.pulses[i] += st.pulses;
 }
 
-static void advance_mixed_range(const Mechanism *m, const Method *me, const Control *ctl, u32 sweeps,
+static void advance_mixed_range(const Mechanism *m, const Method *me, const Control *ctl, u32 sweeps, u32 variant,
                                 const LaneArrays *a, u32 begin, u32 end, double duration) {
     MixedWork w;
     w.size(*m);
     std::vector<double> y(m->n());
-    for (u32 i = begin; i < end; ++i) advance_mixed_lane(*m, *me, *ctl, sweeps, *a, i, duration, w, y);
+    std::vector<Df2> yd(m->n());
+    for (u32 i = begin; i < end; ++i) {
+        if (variant == 1) advance_mixed_df_lane(*m, *me, *ctl, *a, i, duration, w, yd);
+        else advance_mixed_lane(*m, *me, *ctl, sweeps, *a, i, duration, w, y);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1309,12 +1467,13 @@ s32 or_advance(void *h, s32 method_id, const Control *ctl, const LaneArrays *arr
     return 0;
 }
 
-// Model of the module's mixed-precision path (see integrate_mixed), lanes [begin, end).
+// Model of the module's mixed-precision path, lanes [begin, end): variant 0 =
+// FP64 state with `sweeps` FP64-residual refinement sweeps (integrate_mixed),
+// variant 1 = double-float state (integrate_mixed_df).
 s32 or_advance_mixed(void *h, s32 method_id, const Control *ctl, const LaneArrays *arrays, u32 begin, u32 end,
-                     double duration, u32 sweeps, u32 scaled, u32 threads) {
+                     double duration, u32 sweeps, u32 variant, u32 threads) {
     Mechanism *m = (Mechanism *)h;
     Method me = method_coefficients(method_id);
-    (void)scaled;
     if (threads == 0) threads = std::thread::hardware_concurrency();
     if (threads == 0) threads = 1;
     if (end <= begin) return 0;
@@ -1328,7 +1487,7 @@ s32 or_advance_mixed(void *h, s32 method_id, const Control *ctl, const LaneArray
                 u32 c = cursor.fetch_add(1);
                 if (c >= nchunk) break;
                 u32 b = begin + c * per, e = std::min(end, b + per);
-                advance_mixed_range(m, &me, ctl, sweeps, arrays, b, e, duration);
+                advance_mixed_range(m, &me, ctl, sweeps, variant, arrays, b, e, duration);
             }
         });
     for (auto &t : pool) t.join();

@@ -223,12 +223,14 @@ class Mechanism:
 
 
 def advance_mixed(mech: "Mechanism", method: str, ctl: Control, block: dict, padded: int, begin: int, end: int,
-                  duration: float, sweeps: int = 1, scaled: int = 1, threads: int = 0) -> None:
-    """Model of the GPU module's mixed-precision path (FP32 chemistry, FP64 residual,
-    state and control); used to check the GPU's mixed kernel bit for bit."""
+                  duration: float, sweeps: int = 1, variant: int = 0, threads: int = 0) -> None:
+    """Model of the GPU module's mixed-precision path; used to check the GPU's mixed
+    kernel bit for bit. variant 0: FP32 chemistry, FP64 residual refinement, FP64
+    state and control; variant 1: double-float state, FP32 stage vectors / LU /
+    solves, double-float stage right-hand sides."""
     la = lane_arrays(block, padded)
     rc = lib().or_advance_mixed(mech.h, METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, sweeps,
-                                scaled, threads)
+                                variant, threads)
     if rc != 0:
         raise RuntimeError(f"or_advance_mixed failed: {rc}")
 

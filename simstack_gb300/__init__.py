@@ -155,6 +155,8 @@ def lib() -> C.CDLL:
             "gpu_kin_autotune": (i32, [C.POINTER(GpuKinLaunch), u32, C.POINTER(GpuKinTuning)]),
             "gpu_kin_last_stats": (i32, [C.POINTER(u64), C.POINTER(f)]),
             "gpu_kin_set_refinement": (i32, [u32]),
+            "gpu_kin_set_mixed_variant": (i32, [u32]),
+            "gpu_kin_get_mixed_variant": (u32, []),
             "gpu_probe_throughput": (i32, [u32, C.POINTER(d)]),
             "gpu_stream": (vp, []),
             "gpu_copy_on_device": (i32, [vp, vp, u64]),
@@ -506,6 +508,13 @@ class Module:
         ms = self.advance(z.launch(base, precision, duration), queue)
         self.download(z, base)
         return ms
+
+    def set_mixed_variant(self, variant: int) -> None:
+        """Precision 2: 0 = FP64 state with an FP64-residual refinement sweep, 1 = double-float state."""
+        check(lib().gpu_kin_set_mixed_variant(variant), "gpu_kin_set_mixed_variant")
+
+    def mixed_variant(self) -> int:
+        return int(lib().gpu_kin_get_mixed_variant())
 
     # cooperative kernels (one CTA per cell): mechanisms beyond the KinMech tables
     def coop_set_mech(self, model: "Model", meth: KinMethod | None = None, ctl: KinControl | None = None) -> None:

@@ -69,6 +69,8 @@ def build(force: bool = False, jobs: int | None = None) -> str:
         ("kern_air_p0.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=0", "-c", os.path.join(CSRC, "kern_air.cu")]),
         ("kern_air_p1.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=1", "-c", os.path.join(CSRC, "kern_air.cu")]),
         ("kern_air_p2.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=2", "-c", os.path.join(CSRC, "kern_air.cu")]),
+        ("kern_air_p3.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=3", "-c", os.path.join(CSRC, "kern_air.cu")]),
+        ("kern_table_p3.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=3", "-c", os.path.join(CSRC, "kern_table.cu")]),
         ("kern_table_p0.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=0", "-c", os.path.join(CSRC, "kern_table.cu")]),
         ("kern_table_p1.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=1", "-c", os.path.join(CSRC, "kern_table.cu")]),
         ("kern_table_p2.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=2", "-c", os.path.join(CSRC, "kern_table.cu")]),

@@ -27,6 +27,10 @@ cudaError_t launch_table_p2(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p0(uint32_t, uint32_t, size_t, int *);
 cudaError_t occupancy_table_p1(uint32_t, uint32_t, size_t, int *);
 cudaError_t occupancy_table_p2(uint32_t, uint32_t, size_t, int *);
+cudaError_t launch_air_p3(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
 uint64_t air_ops_signature();
 cudaError_t run_probe(uint32_t kind, int sms, cudaStream_t stream, double *ops_per_s);
 }   // namespace sgb
@@ -53,6 +57,7 @@ struct Module {
     uint32_t mode = 0;
     GpuKinTuning tuning[3];
     uint32_t ir_sweeps = 1;
+    uint32_t mixed_variant = 0;    // precision 2: 0 FP64-residual refinement, 1 double-float state
     uint64_t launches = 0;
     float last_ms = 0.0f;
 };
@@ -85,6 +90,9 @@ void fill_args(const GpuKinLaunch *L, DevArgs *A) {
 }
 
 cudaError_t occupancy(uint32_t prec, const GpuKinTuning &t, int *blocks) {
+    if (prec == 2 && g.mixed_variant == 1)
+        return g.generated ? occupancy_air_p3(t.kind, t.variant, t.block, blocks)
+                           : occupancy_table_p3(t.kind, t.block, kTableBytes, blocks);
     if (g.generated) {
         if (prec == 0) return occupancy_air_p0(t.kind, t.variant, t.block, blocks);
         if (prec == 1) return occupancy_air_p1(t.kind, t.variant, t.block, blocks);
@@ -116,6 +124,11 @@ cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &
         s.grid = resident < needed ? resident : needed;
         e = cudaMemsetAsync(g.d_cursor, 0, sizeof(uint32_t), g.stream);
         if (e != cudaSuccess) return e;
+    }
+    if (prec == 2 && g.mixed_variant == 1) {
+        if (g.generated) return launch_air_p3(s, A, g.stream);
+        s.variant = 0;
+        return launch_table_p3(s, A, g.stream);
     }
     if (g.generated) {
         if (prec == 0) return launch_air_p0(s, A, g.stream);
@@ -470,6 +483,14 @@ SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps) {
     g.ir_sweeps = sweeps;
     return 0;
 }
+
+SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant) {
+    if (variant > 1) return (int32_t)cudaErrorInvalidValue;
+    g.mixed_variant = variant;
+    return 0;
+}
+
+SGB_API uint32_t gpu_kin_get_mixed_variant(void) { return g.mixed_variant; }
 
 // Measured instruction throughput (operations per second over the device):
 // kind 0 DFMA, 1 FFMA, 2 FP32<->FP64 conversion pairs, 3 DADD, 4 FP64 reciprocal, 5 FP64 sqrt.

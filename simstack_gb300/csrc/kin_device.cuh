@@ -557,6 +557,271 @@ struct Lane {
 };
 
 // ---------------------------------------------------------------------------
+// Mixed path, double-float state: the whole step on the FP32 pipe. The state
+// y and the RHS at the step start are double-float (hi + lo, ~48-bit
+// significand); the Jacobian, LU, stage vectors K and solves are FP32; the
+// stage right-hand sides f(y) + [f(Y) - f(y)] + sum c/h K_j are accumulated in
+// double-float before rounding to FP32, so the cancellation between f(y) and
+// the stage terms costs no FP32 accuracy; y_new = y + sum m K in
+// double-float. Only the scalar controller (t, h) stays FP64. FP64 arithmetic
+// is 1/74 of FP32 on this GPU and conversions between the two run at the FP64
+// rate, so this path issues almost no FP64 work per species.
+
+__device__ __forceinline__ Df df_add_f(Df a, float b) {   // a + b, b a float (two-sum of the high parts)
+    const float s = a.hi + b;
+    const float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (b - bb);
+    e = e + a.lo;
+    const float t = s + e;
+    return Df{t, e - (t - s)};
+}
+__device__ __forceinline__ Df df_prod_f(float a, float b) {   // exact product of two floats
+    const float p = a * b;
+    return Df{p, fmaf(a, b, -p)};
+}
+
+template <class Ops, class M>
+struct LaneDf {
+    static constexpr int N = Ops::N, R = Ops::R, NNZ = Ops::NNZ, S = M::kStages;
+
+    Ops ops;
+    float yhi[N], ylo[N];
+    float khi[R], klo[R], shi[N], slo[N];
+    double t, h, seg_end, applied, duration, period, first, count;
+    double steps, rejects, pulses, failed;
+    uint32_t iterations, transitions;
+    int phase;
+    bool pending, reject_last, reject_more;
+    float lu[NNZ];
+    float fhi[N], flo[N];
+    float K[S][N];
+    float d32[N], df32[N];
+    float nhi[N], nlo[N];
+
+    __device__ __forceinline__ uint32_t n() const { return ops.n(); }
+
+    __device__ __forceinline__ void load(const DevArgs &A, uint32_t i) {
+        const uint32_t p = A.padded, nn = n(), rr_ = ops.r();
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            Df v = df_from(A.y[(size_t)s * p + i]);
+            yhi[s] = v.hi;
+            ylo[s] = v.lo;
+            v = df_from(A.src[(size_t)s * p + i]);
+            shi[s] = v.hi;
+            slo[s] = v.lo;
+        }
+        for (int r = 0; r < R; ++r) {
+            if (r >= (int)rr_) break;
+            const Df v = df_from(A.k[(size_t)r * p + i]);
+            khi[r] = v.hi;
+            klo[r] = v.lo;
+        }
+        h = A.h[i];
+        period = A.period[i];
+        first = A.pulse_first[i];
+        count = A.pulse_count[i];
+        duration = A.duration;
+        steps = rejects = pulses = 0.0;
+        failed = A.failed[i];
+        t = 0.0;
+        applied = 0.0;
+        transitions = 0;
+        phase = kPhaseSegStart;
+    }
+
+    __device__ __forceinline__ void store(const DevArgs &A, uint32_t i) {
+        const uint32_t p = A.padded, nn = n();
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            A.y[(size_t)s * p + i] = df_to(Df{yhi[s], ylo[s]});
+        }
+        A.h[i] = h;
+        A.failed[i] = failed;
+        A.steps[i] += steps;
+        A.rejects[i] += rejects;
+        A.pulses[i] += pulses;
+    }
+
+    __device__ __forceinline__ void seg_start(const DevArgs &A) {
+        pending = applied < count;
+        double next_pulse = sgb_fma(applied, period, first);
+        seg_end = pending ? vmin(next_pulse, duration) : duration;
+        bool active = t < seg_end && !(failed > 0.0);
+        reject_last = false;
+        reject_more = false;
+        h = h > 0.0 ? h : A.ctl.h_start;
+        iterations = 0;
+        phase = active ? kPhaseStepping : kPhaseSegFinish;
+    }
+
+    __device__ __forceinline__ void seg_finish(const DevArgs &A, uint32_t cell) {
+        bool alive = !(failed > 0.0);
+        bool hit = pending && alive && t >= seg_end;
+        if (hit) {
+            const uint32_t p = A.padded, nn = n();
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                const Df v = df_add(Df{yhi[s], ylo[s]}, df_from(A.pulse[(size_t)s * p + cell]));
+                yhi[s] = v.hi;
+                ylo[s] = v.lo;
+            }
+            applied = applied + 1.0;
+            pulses = pulses + 1.0;
+            h = A.ctl.h_start;
+        }
+        bool done = (t >= duration && applied >= count) || !alive;
+        phase = done ? kPhaseDone : kPhaseSegStart;
+    }
+
+    __device__ __forceinline__ bool settle(const DevArgs &A, uint32_t cell) {
+        for (;;) {
+            if (++transitions > (1u << 24)) {
+                failed = 1.0;
+                phase = kPhaseDone;
+            }
+            switch (phase) {
+                case kPhaseSegStart: seg_start(A); break;
+                case kPhaseSegFinish: seg_finish(A, cell); break;
+                case kPhaseStepping:
+                    if (++iterations > A.ctl.max_steps) {
+                        failed = 1.0;
+                        phase = kPhaseSegFinish;
+                        break;
+                    }
+                    return true;
+                default: return false;
+            }
+        }
+    }
+
+    template <bool kSync = false>
+    __device__ __forceinline__ void attempt(const DevArgs &A, bool commit = true) {
+        const uint32_t nn = n();
+        const float rtol = (float)A.ctl.rtol, atol = (float)A.ctl.atol;
+        const float inv_n = 1.0f / (float)nn;
+
+        const double remaining = seg_end - t;
+        double h_cap = remaining;
+        if (A.ctl.h_max > 0.0) h_cap = vmin(h_cap, A.ctl.h_max);
+        const double h_wanted = vmax(h, A.ctl.h_min);
+        const bool last = h_wanted >= remaining;
+        const double hs = last ? remaining : vmin(h_wanted, h_cap);
+        const float hs32 = (float)hs;
+
+        ops.fun_df(khi, klo, shi, slo, yhi, ylo, fhi, flo);
+        ops.neg_jac(khi, yhi, lu);
+        if constexpr (kSync) __syncthreads();
+        ops.factor(1.0f / (hs32 * (float)M::gamma0(A)), lu);
+        if constexpr (kSync) __syncthreads();
+        const float hinv = 1.0f / hs32;
+
+        bool last_moved = false;
+#pragma unroll 1
+        for (int st = 0; st < S; ++st) {
+            if (st >= M::stages(A)) break;
+            const int packed = st * (st - 1) / 2;
+            if (st > 0 && M::new_f(A, st)) {
+                bool moved = false;
+                for (int s = 0; s < N; ++s) {
+                    if (s >= (int)nn) break;
+                    d32[s] = 0.0f;
+                }
+#pragma unroll
+                for (int j = 0; j < st; ++j) {
+                    const float av = (float)M::a(A, packed + j);
+                    if (av == 0.0f) continue;
+                    moved = true;
+                    for (int s = 0; s < N; ++s) {
+                        if (s >= (int)nn) break;
+                        d32[s] = fmaf(av, K[j][s], d32[s]);
+                    }
+                }
+                if (moved) ops.fun_delta(khi, yhi, d32, df32);
+                last_moved = moved;
+            }
+            // b = f(y) [+ f(Y) - f(y)] + sum_j c_j / h K_j in double-float, rounded once
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                Df b{fhi[s], flo[s]};
+                if (last_moved) b = df_add_f(b, df32[s]);
+#pragma unroll
+                for (int j = 0; j < st; ++j) {
+                    const float c = (float)M::c(A, packed + j);
+                    if (c == 0.0f) continue;
+                    b = df_add(b, df_prod_f(c * hinv, K[j][s]));
+                }
+                K[st][s] = b.hi + b.lo;
+            }
+            ops.solve(lu, K[st]);
+            if constexpr (kSync) __syncthreads();
+        }
+
+        // y_new (double-float) and the weighted RMS error (FP32)
+        float err32 = 0.0f;
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            Df yn{yhi[s], ylo[s]};
+            float yerr = 0.0f;
+#pragma unroll
+            for (int st = 0; st < S; ++st) {
+                if (st >= M::stages(A)) break;
+                const float mc = (float)M::m(A, st), ec = (float)M::e(A, st);
+                if (mc != 0.0f) yn = df_add(yn, df_prod_f(mc, K[st][s]));
+                if (ec != 0.0f) yerr = fmaf(ec, K[st][s], yerr);
+            }
+            const float scale = fmaf(rtol, fmaxf(fabsf(yhi[s]), fabsf(yn.hi)), atol);
+            const float q = yerr / scale;
+            err32 = fmaf(q, q, err32);
+            nhi[s] = yn.hi;
+            nlo[s] = yn.lo;
+        }
+        err32 = sqrtf(err32 * inv_n);
+        if (!is_finite_lane(err32)) err32 = 1e10f;
+        float fac32 = step_factor(err32, M::order(A));
+        bool ok = err32 <= 1.0f || hs <= A.ctl.h_min;
+        if (A.ctl.fixed_step) {
+            ok = true;
+            fac32 = 1.0f;
+        }
+        if (!commit) return;
+        if (ok) {
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                float hi = nhi[s], lo = nlo[s];
+                if (A.ctl.clamp_negative && (hi < 0.0f || (hi == 0.0f && lo < 0.0f))) {
+                    hi = 0.0f;
+                    lo = 0.0f;
+                }
+                yhi[s] = hi;
+                ylo[s] = lo;
+            }
+            t = last ? seg_end : t + hs;
+        }
+        const double fac = (double)fac32;
+        double h_acc = hs * fac;
+        h_acc = reject_last ? vmin(h_acc, hs) : h_acc;
+        h_acc = (last && fac >= 1.0) ? vmax(h_acc, h_wanted) : h_acc;
+        double h_rej = reject_more ? hs * 0.1 : vmin(hs * fac, hs);
+        if (A.ctl.fixed_step) {
+            h_acc = h_wanted;
+            h_rej = h_wanted;
+        }
+        h = ok ? h_acc : h_rej;
+        reject_more = !ok && reject_last;
+        reject_last = !ok;
+        steps = steps + (ok ? 1.0 : 0.0);
+        rejects = rejects + (ok ? 0.0 : 1.0);
+        if (!(t < seg_end && !(failed > 0.0))) phase = kPhaseSegFinish;
+    }
+};
+
+// The lane type of a precision: 0 FP64, 1 f32 Delta, 2 mixed with FP64
+// refinement, 3 mixed with double-float state.
+template <class Ops, class M, int PREC> struct LaneOf { typedef Lane<Ops, M, PREC> type; };
+template <class Ops, class M> struct LaneOf<Ops, M, 3> { typedef LaneDf<Ops, M> type; };
+
+// ---------------------------------------------------------------------------
 // Generated straight-line ops (kin_codegen.cpp) as an Ops object.
 
 // SGB_OPS_QUALIFIER: __forceinline__ (default) inlines every op at every call

@@ -33,7 +33,7 @@ template <> struct Budget<2> { static constexpr int kThreads = 256, kMinBlocks =
 template <class Ops, class M, int PREC, int V>
 __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_static_kernel(const __grid_constant__ DevArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
-    Lane<Ops, M, PREC> L;
+    typename LaneOf<Ops, M, PREC>::type L;
     if (!L.ops.init(A, smem)) {
         if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
         return;
@@ -58,7 +58,7 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
 template <class Ops, class M, int PREC, int V>
 __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_queue_kernel(const __grid_constant__ DevArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
-    Lane<Ops, M, PREC> L;
+    typename LaneOf<Ops, M, PREC>::type L;
     if (!L.ops.init(A, smem)) {
         if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
         return;
@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
 template <class Ops, class M, int PREC, int V>
 __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_queue_cta_kernel(const __grid_constant__ DevArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
-    Lane<Ops, M, PREC> L;
+    typename LaneOf<Ops, M, PREC>::type L;
     if (!L.ops.init(A, smem)) {
         if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
         return;
