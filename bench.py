@@ -320,6 +320,17 @@ def run_ours(args):
     steps_total = float(zc["steps"][:cells].sum() + zc["rejects"][:cells].sum())
     failed = int(zc["failed"][:cells].sum())
 
+    # the mixed path's other variant (FP64 state + FP64-residual refinement), for comparison
+    variant_default = mod.mixed_variant()
+    mod.set_mixed_variant(0)
+    restore()
+    launch.precision = 2
+    t_v0 = mod.autotune(launch, kind=2)
+    wall_v0, kern_v0, _ = timed_pass(2, args.steps, 1)
+    zv0 = z.copy()
+    mod.download(zv0, work)
+    mod.set_mixed_variant(variant_default)
+
     # autotune the launch shape once per precision (persistent queue kernel)
     tuned = {}
     for prec in (0, 2):
@@ -344,6 +355,8 @@ def run_ours(args):
     with np.errstate(all="ignore"):
         rel_sig = (np.abs(ya - yb) / np.abs(yb))[sig_mask]
     flips = float(np.mean((zm["steps"][:cells] != zc["steps"][:cells]) | (zm["rejects"][:cells] != zc["rejects"][:cells])))
+    with np.errstate(all="ignore"):
+        rel_sig_v0 = (np.abs(zv0["y"][:, :cells] - yb) / np.abs(yb))[sig_mask]
 
     # end-to-end through the C ABI with host buffers (pinned), per step
     sg.check(L.gpu_host_register(z.data.ctypes.data, z.nbytes), "gpu_host_register")
@@ -416,18 +429,36 @@ def run_ours(args):
                   "rel_err_vs_fp64_atol_floored": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
                                                    "definition": "|a-b|/max(|b|, atol) over every species and cell"},
                   "cells_with_different_step_counts": flips,
-                  "reference_for_errors": "the FP64 path on the same batch, bit-identical to the reference CPU solver"},
+                  "reference_for_errors": "the FP64 path on the same batch, bit-identical to the reference CPU solver",
+                  "variant": "double-float state (hi+lo FP32 pairs), FP32 Jacobian / LU / stage vectors / solves, "
+                             "double-float stage right-hand sides; FP64 only in the scalar step controller"
+                             if variant_default == 1 else "FP64 state, FP32 LU, one FP64-residual refinement sweep",
+                  "other_variant": {"variant": "FP64 state, FP32 Jacobian / LU / solves, one FP64-residual refinement "
+                                               "sweep per stage, double-float f(y)" if variant_default == 1 else
+                                               "double-float state",
+                                    "kernel_ms": float(np.mean(kern_v0)),
+                                    "value": total_cells / (grp.max(wall_v0 / args.steps * 1e3) * 1e-3),
+                                    "speedup_vs_fp64": ms64 / float(np.mean(kern_v0)),
+                                    "rel_err_vs_fp64": {"max": float(rel_sig_v0.max()),
+                                                        "p99": float(np.quantile(rel_sig_v0, 0.99))},
+                                    "tuning": {"block": t_v0.block, "variant": t_v0.variant, "ctas_per_sm": t_v0.chunk}}},
         "steps_per_cell": {"mean": steps_total / cells, "failed_cells": failed},
-        "roofline": {"bound": "fp64", "achieved": ach64 if head == "f64" else achmx, "peak": fp64_peak,
-                     "unit": "TFLOP/s", "frac": (ach64 if head == "f64" else achmx) / fp64_peak,
+        "roofline": {"bound": "fp64" if head == "f64" else "fp32",
+                     "achieved": ach64 if head == "f64" else achmx,
+                     "peak": fp64_peak if head == "f64" else fp32_peak,
+                     "unit": "TFLOP/s",
+                     "frac": ach64 / fp64_peak if head == "f64" else achmx / fp32_peak,
                      "traffic": DRAM_BYTES_PER_CELL_STEP[head] * steps_total,
                      "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per launch: the per-cell-step "
                                      "figure of one ncu capture (262,144 cells x 0.5 s) x this launch's attempted "
                                      "cell-steps (FP64-path counts); local-memory spills, not algorithmic bytes",
-                     "peak_source": "FP64 FMA throughput measured in this run (gpu_probe_throughput kind 0), x2 flops",
+                     "peak_source": "FMA throughput measured in this run (gpu_probe_throughput kind 0 FP64, "
+                                    "kind 1 FP32), x2 flops",
                      "algorithmic_flops_per_step": flops["total"],
                      "note": "algorithmic flops = FP64 path step count (= the oracle's) x flops per Rodas3 step; "
-                             "the mixed path does most of them in FP32",
+                             "the mixed path does them on the FP32 pipe, in double-float where precision needs it "
+                             "(several FP32 instructions per algorithmic flop), so its fraction of the FP32 peak "
+                             "understates the pipe's use; mixed_path.frac_of_fp64_peak is the FP64-equivalent rate",
                      "fp64_path": {"achieved": ach64, "frac": ach64 / fp64_peak},
                      "mixed_path": {"achieved": achmx, "frac_of_fp64_peak": achmx / fp64_peak,
                                     "frac_of_fp32_peak": achmx / fp32_peak, "fp32_peak": fp32_peak},

@@ -212,7 +212,7 @@ SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps);
 /* Mixed path (precision 2) variant: 0 = FP32 Jacobian / LU / solves with an FP64-residual refinement
  * sweep per stage, FP64 state; 1 = double-float state (hi + lo FP32 pairs) with FP32 stage vectors,
  * LU and solves, stage right-hand sides accumulated in double-float, almost no FP64 work per species
- * (only the scalar step controller stays FP64). */
+ * (only the scalar step controller stays FP64). Default 1. */
 SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant);
 SGB_API uint32_t gpu_kin_get_mixed_variant(void);
 

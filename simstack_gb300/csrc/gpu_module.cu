@@ -57,7 +57,7 @@ struct Module {
     uint32_t mode = 0;
     GpuKinTuning tuning[3];
     uint32_t ir_sweeps = 1;
-    uint32_t mixed_variant = 0;    // precision 2: 0 FP64-residual refinement, 1 double-float state
+    uint32_t mixed_variant = 1;    // precision 2: 0 FP64-residual refinement, 1 double-float state (default)
     uint64_t launches = 0;
     float last_ms = 0.0f;
 };

@@ -53,6 +53,10 @@ cudaError_t launch_table_p2(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p0(uint32_t, uint32_t, size_t, int *);
 cudaError_t occupancy_table_p1(uint32_t, uint32_t, size_t, int *);
 cudaError_t occupancy_table_p2(uint32_t, uint32_t, size_t, int *);
+cudaError_t launch_air_p3(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
 uint64_t air_ops_signature();
 }   // namespace sgb
 
@@ -168,17 +172,19 @@ Engine E;
 
 uint32_t pad8(uint32_t c) { return (c + 7u) / 8u * 8u; }
 
+// p: 0 FP64, 1 f32 Delta, 2 mixed with FP64 refinement, 3 mixed with double-float state
 cudaError_t launch_chem(bool generated, uint32_t p, const Shape &sh, const DevArgs &A, cudaStream_t s) {
-    if (generated) return p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : launch_air_p2(sh, A, s);
-    return p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : launch_table_p2(sh, A, s);
+    if (generated)
+        return p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : p == 2 ? launch_air_p2(sh, A, s) : launch_air_p3(sh, A, s);
+    return p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : p == 2 ? launch_table_p2(sh, A, s) : launch_table_p3(sh, A, s);
 }
 
 cudaError_t occupancy_chem(bool generated, uint32_t p, uint32_t block, size_t smem, int *per_sm) {
     if (generated)
         return p == 0 ? occupancy_air_p0(2, 0, block, per_sm) : p == 1 ? occupancy_air_p1(2, 0, block, per_sm)
-                                                                       : occupancy_air_p2(2, 0, block, per_sm);
+               : p == 2 ? occupancy_air_p2(2, 0, block, per_sm) : occupancy_air_p3(2, 0, block, per_sm);
     return p == 0 ? occupancy_table_p0(2, block, smem, per_sm) : p == 1 ? occupancy_table_p1(2, block, smem, per_sm)
-                                                                       : occupancy_table_p2(2, block, smem, per_sm);
+           : p == 2 ? occupancy_table_p2(2, block, smem, per_sm) : occupancy_table_p3(2, block, smem, per_sm);
 }
 
 // Frees a request's device resources in stream order (no device-wide synchronisation).
@@ -264,7 +270,9 @@ cudaError_t admit(Request *r) {
     sh.variant = 0;
     sh.smem = r->generated ? 0 : kTableBytes;
     int per_sm = 0;
-    e = occupancy_chem(r->generated, q.precision, sh.block, sh.smem, &per_sm);
+    // precision 2 runs the module's current mixed variant (gpu_kin_set_mixed_variant), fixed at admission
+    const uint32_t kp = q.precision == 2 && gpu_kin_get_mixed_variant() == 1 ? 3u : q.precision;
+    e = occupancy_chem(r->generated, kp, sh.block, sh.smem, &per_sm);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     const uint32_t resident = (uint32_t)per_sm * (uint32_t)E.sms, needed = (q.cells + sh.block - 1) / sh.block;
@@ -274,7 +282,7 @@ cudaError_t admit(Request *r) {
     // its attributes (it returns right after staging its tables)
     DevArgs idle = A;
     idle.lanes = 0;
-    e = launch_chem(r->generated, q.precision, sh, idle, r->stream);
+    e = launch_chem(r->generated, kp, sh, idle, r->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
     if (e != cudaSuccess) return e;
 
@@ -282,7 +290,7 @@ cudaError_t admit(Request *r) {
     e = cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal);
     if (e != cudaSuccess) return e;
     cudaError_t ce = cudaMemsetAsync(r->d_scratch, 0, sizeof(uint32_t), r->stream);   // the cursor; the error flag stays sticky
-    if (ce == cudaSuccess) ce = launch_chem(r->generated, q.precision, sh, A, r->stream);
+    if (ce == cudaSuccess) ce = launch_chem(r->generated, kp, sh, A, r->stream);
     if (ce == cudaSuccess)
         ce = (cudaError_t)gpu_advect(A.y, P, r->n, q.cells, q.channel_cells, r->d_inlet, r->courant, r->substeps, r->stream);
     e = cudaStreamEndCapture(r->stream, &graph);

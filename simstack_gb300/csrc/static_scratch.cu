@@ -40,6 +40,10 @@ cudaError_t launch_table_p2(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p0(uint32_t, uint32_t, size_t, int *);
 cudaError_t occupancy_table_p1(uint32_t, uint32_t, size_t, int *);
 cudaError_t occupancy_table_p2(uint32_t, uint32_t, size_t, int *);
+cudaError_t launch_air_p3(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
 uint64_t air_ops_signature();
 }   // namespace sgb
 
@@ -144,17 +148,18 @@ SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *me
     sh.block = 128;
     sh.variant = 0;
     sh.smem = generated ? 0 : kTableBytes;
-    const uint32_t p = L->precision;
+    // precision 2 runs the module's current mixed variant (gpu_kin_set_mixed_variant)
+    const uint32_t p = L->precision == 2 && gpu_kin_get_mixed_variant() == 1 ? 3u : L->precision;
     if (generated) e = p == 0 ? occupancy_air_p0(1, 0, sh.block, &per_sm) : p == 1 ? occupancy_air_p1(1, 0, sh.block, &per_sm)
-                                                                                  : occupancy_air_p2(1, 0, sh.block, &per_sm);
+                       : p == 2 ? occupancy_air_p2(1, 0, sh.block, &per_sm) : occupancy_air_p3(1, 0, sh.block, &per_sm);
     else e = p == 0 ? occupancy_table_p0(1, sh.block, sh.smem, &per_sm) : p == 1 ? occupancy_table_p1(1, sh.block, sh.smem, &per_sm)
-                                                                              : occupancy_table_p2(1, sh.block, sh.smem, &per_sm);
+             : p == 2 ? occupancy_table_p2(1, sh.block, sh.smem, &per_sm) : occupancy_table_p3(1, sh.block, sh.smem, &per_sm);
     if (e != cudaSuccess) return (int32_t)e;
     if (per_sm < 1) per_sm = 1;
     const uint32_t resident = (uint32_t)per_sm * (uint32_t)sms, needed_ctas = (A.lanes + sh.block - 1) / sh.block;
     sh.grid = resident < needed_ctas ? resident : needed_ctas;
-    if (generated) e = p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : launch_air_p2(sh, A, s);
-    else e = p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : launch_table_p2(sh, A, s);
+    if (generated) e = p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : p == 2 ? launch_air_p2(sh, A, s) : launch_air_p3(sh, A, s);
+    else e = p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : p == 2 ? launch_table_p2(sh, A, s) : launch_table_p3(sh, A, s);
     if (e != cudaSuccess) return (int32_t)e;
     if (!wait) return 0;
     uint32_t flag = 0;

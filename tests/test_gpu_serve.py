@@ -21,8 +21,9 @@ def oracle_coupled(O, z, cells, channel_cells, steps, courant, substeps, method=
     ctl = O.control()
     inlet = np.array(z["y"][:, 0])
     for _ in range(steps):
-        if precision == 2:
-            O.advance_mixed(mech, method, ctl, z.as_dict(), z.padded, 0, cells, 1.0, sweeps=1)
+        if precision == 2:   # the module's current mixed variant
+            O.advance_mixed(mech, method, ctl, z.as_dict(), z.padded, 0, cells, 1.0, sweeps=1,
+                            variant=int(sg.lib().gpu_kin_get_mixed_variant()))
         else:
             mech.advance(method, ctl, z.as_dict(), z.padded, 0, cells, 1.0, precision, 1)
         y = z["y"]
