@@ -53,11 +53,14 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--workload", choices=["config2", "config1", "config3", "config5"], default="config2",
+    ap.add_argument("--workload", choices=["config2", "config1", "config3", "config4", "config5"], default="config2",
                     help="config2 (default, the headline): 1,048,576 cells x 10 s; config1: 4,096 cells x 1 s; "
                          "config3: uneven stiffness, 262,144 cells x 60 s with a discharge source, static vs queue; "
+                         "config4: 200-species / 1,200-reaction synthetic mechanism, one CTA per cell; "
                          "config5: served requests (Poisson arrivals) with film advection, p50/p99 latency")
     ap.add_argument("--requests", type=int, default=48, help="config5: requests in the served sample")
+    ap.add_argument("--fp64-cells", type=int, default=1216,
+                    help="config4: cells of the FP64 comparison sample (the first cells of the workload)")
     ap.add_argument("--profile-case", choices=["f64", "mixed", "f32"], default=None,
                     help="one queue-kernel advance of --cells x --duration at this precision, then exit (ncu captures)")
     return ap.parse_args()
@@ -528,6 +531,95 @@ def run_config3(args):
     print(json.dumps(line))
 
 
+def run_config4(args):
+    """Large synthetic mechanism through the cooperative kernels: mixed on --cells cells (default 65,536),
+    FP64 (bit-identical to the reference's algorithm) on the first --fp64-cells of them."""
+    import simstack_gb300 as sg
+    from oracle import oracle as O   # the CPU baseline leg only
+
+    cells = args.cells if args.cells != (1 << 20) else 65536
+    duration = args.duration
+    pm = sg.Model.synthetic(seed=args.seed, species=200, reactions=1200, bimolecular=0.7, products=1,
+                            lk_lo=-3.0, lk_hi=9.0)
+    ctl = sg.control(rtol=1e-4, atol=1e-12, h_min=1e-14, h_start=1e-9, max_steps=200000)
+    z = sg.synthetic_cells(pm, cells, seed=args.seed + 1, log10_c=(-10.0, -3.0))
+    mod = sg.Module(0, 2 * z.nbytes + (256 << 20))
+    mod.coop_set_mech(pm, sg.method("rodas3"), ctl)
+    info = mod.coop_info()
+    base = mod.upload(z)
+    nf = min(args.fp64_cells, cells)
+    zf = z.copy()
+    # FP64 on the sample (its own lane count), then mixed on everything; warm-up on a few cells first
+    mod.coop_advance(z.launch(base, 2, duration, lane_count=min(cells, 152)))
+    sg.check(sg.lib().gpu_copy_to_device(base, z.data.ctypes.data, z.nbytes), "restore")
+    clocks = ClockSampler(0)
+    clocks.start()
+    ms64 = mod.coop_advance(z.launch(base, 0, duration, lane_count=nf))
+    mod.download(zf, base)
+    sg.check(sg.lib().gpu_copy_to_device(base, z.data.ctypes.data, z.nbytes), "restore")
+    msmx = mod.coop_advance(z.launch(base, 2, duration))
+    clk = clocks.stop()
+    zm = z.copy()
+    mod.download(zm, base)
+    a, b = zm["y"][:, :nf], zf["y"][:, :nf]
+    sig = b >= 1e-9 * b.sum(axis=0)
+    with np.errstate(all="ignore"):
+        rel = (np.abs(a - b) / np.abs(b))[sig]
+    steps64 = float(zf["steps"][:nf].sum() + zf["rejects"][:nf].sum())
+    stepsmx = float(zm["steps"][:cells].sum() + zm["rejects"][:cells].sum())
+    # algorithmic flops per Rodas3 step: LU 2 per update + 4 divisions, 4 solves over the L and U
+    # entries (2 flops each) + n multiplies, 4 RHS (a multiply per reactant, 2 flops per term),
+    # the Jacobian (2 flops per term + products), stage combination and error ~ 12 n
+    n, R = info["n"], info["R"]
+    flops_step = (2 * info["lu_updates"] + 4 * n + 4 * (2 * (info["l_entries"] + info["u_entries"]) + n)
+                  + 4 * (int(1.7 * R) + 2 * 2 * R) + 2 * 2 * info["jac_entries"] + 12 * n)
+    dfma = mod.probe(0)
+    ffma = mod.probe(1)
+    v64 = nf / (ms64 * 1e-3)
+    vmx = cells / (msmx * 1e-3)
+    # CPU: the oracle (the reference's algorithm with 32-bit indices) on a bounded sample, all host threads
+    om = O.Mechanism()
+    for sp in range(n):
+        om.add_species(f"S{sp}", True)
+    for r in range(R):
+        om.add_reaction(sg.model_equation(pm, r), "arr", (float(pm.k_const[r]), 0.0, 0.0))
+    om.finalize()
+    threads = os.cpu_count() or 1
+    ncpu = min(cells, 2 * threads)
+    zc = z.copy()
+    t0 = time.perf_counter()
+    om.advance("rodas3", O.control(rtol=1e-4, atol=1e-12, h_min=1e-14, h_start=1e-9, max_steps=200000), zc.as_dict(),
+               zc.padded, 0, ncpu, duration, 0, threads)
+    cpu_s = time.perf_counter() - t0
+    cpu_ok = zc["y"][:, :min(ncpu, nf)].tobytes() == zf["y"][:, :min(ncpu, nf)].tobytes()
+    line = {"metric": "cell-integrations/s", "value": vmx, "unit": "cell-integrations/s", "n_gpus": 1, "steps": 1,
+            "warmup": 1, "ms_per_step": msmx, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32+f64", "data": "synthetic",
+            "config": {"workload": f"synthetic mechanism: 200 species, 1,200 reactions (70% bimolecular, 1 product, "
+                                   f"k 10^U[-3,9]), {cells} cells x {duration:g} s, c 10^U[-10,-3], rtol 1e-4, "
+                                   f"atol 1e-12, Rodas3; one CTA per cell", "mechanism": info},
+            "fp64": {"value": v64, "kernel_ms": ms64, "cells": nf,
+                     "parity": "bit-identical to the oracle (tests/test_gpu_coop.py) and to the reference's own "
+                               "solver on a 60-species mechanism",
+                     "achieved_tflops": steps64 * flops_step / (ms64 * 1e-3) / 1e12,
+                     "frac_of_fp64_peak": steps64 * flops_step / (ms64 * 1e-3) / (2 * dfma)},
+            "mixed": {"value": vmx, "kernel_ms": msmx, "speedup_vs_fp64": vmx / v64,
+                      "rel_err_vs_fp64": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+                                          "cells": nf, "definition": "species >= 1e-9 of the cell total"},
+                      "achieved_tflops_fp64_equivalent": stepsmx * flops_step / (msmx * 1e-3) / 1e12,
+                      "frac_of_fp32_peak": stepsmx * flops_step / (msmx * 1e-3) / (2 * ffma)},
+            "steps_per_cell": {"fp64_mean": steps64 / nf, "mixed_mean": stepsmx / cells},
+            "algorithmic_flops_per_step": flops_step,
+            "roofline": {"bound": "fp32", "achieved": stepsmx * flops_step / (msmx * 1e-3) / 1e12,
+                         "peak": 2 * ffma / 1e12, "unit": "TFLOP/s",
+                         "frac": stepsmx * flops_step / (msmx * 1e-3) / (2 * ffma), "traffic": None},
+            "cpu_baseline": {"value": ncpu / cpu_s, "unit": "cell-integrations/s", "cores": threads, "kind": "port",
+                             "sample": f"first {ncpu} cells, {duration:g} s each, oracle/kin_oracle.cpp on {threads} "
+                                       f"host threads ({cpu_s:.1f} s); same bits as the GPU FP64 path: {cpu_ok}"},
+            "gpu_launches": 3, "clocks": clk}
+    print(json.dumps(line))
+
+
 def serve_sample(seed: int, count: int, rate_hz: float = 200.0):
     """The served request stream: Poisson arrivals at rate_hz; cells 10^U[log10 1024, log10 65536];
     horizon 10^U[0, log10 600] s in 1 s coupling steps (log-uniform); channel cells U{256..4096};
@@ -631,6 +723,8 @@ if __name__ == "__main__":
         run_config3(a)
     elif a.workload == "config5" and a.impl == "ours":
         run_config5(a)
+    elif a.workload == "config4" and a.impl == "ours":
+        run_config4(a)
     elif a.impl == "reference":
         run_reference(a)
     else:

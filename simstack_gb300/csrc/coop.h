@@ -9,10 +9,14 @@
 //   - LU: the elimination runs pivot by pivot (KIJ) instead of row by row
 //     (IKJ), which applies the same updates to every element in the same
 //     (ascending pivot) order, so the results are the same bits;
-//   - solves: column-oriented, which gives every x[i] its updates in the
-//     reference's order (lower rows ascending, upper rows descending column).
+//   - solves: in blocks of 32 columns (a warp solves the diagonal block, then
+//     every row outside it takes the block's updates one by one), which gives
+//     every x[i] its updates in the reference's order (lower: ascending
+//     column; upper: descending column, then the diagonal).
 // The LU lives in a dense [n][ld] array (the filled pattern is 78-87% dense
-// for a 200-species random mechanism in natural order).
+// for a 200-species random mechanism in natural order); the kernels walk it
+// densely and test each element against the pattern bitmask, so only
+// pattern elements are ever updated, as in the reference.
 #pragma once
 #include <stdint.h>
 
@@ -46,7 +50,9 @@ struct CoopMech {
     uint32_t off_ucol;        // uint16[]: columns j > k with (k, j) in the filled pattern, per row k
     uint32_t off_cbeg;        // uint32[n+1]
     uint32_t off_crow;        // uint16[]: rows i < k with (i, k) in the filled pattern, per column k
-    uint32_t reserved[3];
+    uint32_t off_pat;         // uint32[n][8]: filled pattern, bit j of row i (n <= 256)
+    uint32_t off_lcnt;        // uint16[n]: rows below the diagonal in column k
+    uint32_t reserved;
 };
 
 }   // namespace sgb

@@ -15,8 +15,8 @@ bool coop_image(const Model &m, std::vector<uint8_t> *out) {
     if (!m.finalized) return false;
     const Symbolic &S = m.sym;
     const uint32_t n = m.n(), R = m.R();
-    if (n == 0 || n > 4096) return false;
-    auto pat = [&](uint32_t i, uint32_t j) { return S.pattern[(size_t)i * n + j] != 0; };
+    if (n == 0 || n > 256) return false;   // pattern rows are 256-bit masks
+    auto pat_at = [&](uint32_t i, uint32_t j) { return S.pattern[(size_t)i * n + j] != 0; };
 
     CoopMech h;
     memset(&h, 0, sizeof(h));
@@ -82,16 +82,24 @@ bool coop_image(const Model &m, std::vector<uint8_t> *out) {
         ubeg[k] = (uint32_t)ucol.size();
         cbeg[k] = (uint32_t)crow.size();
         for (uint32_t i = k + 1; i < n; ++i)
-            if (pat(i, k)) lrow.push_back((uint16_t)i);
+            if (pat_at(i, k)) lrow.push_back((uint16_t)i);
         for (uint32_t j = k + 1; j < n; ++j)
-            if (pat(k, j)) ucol.push_back((uint16_t)j);
+            if (pat_at(k, j)) ucol.push_back((uint16_t)j);
         for (uint32_t i = 0; i < k; ++i)
-            if (pat(i, k)) crow.push_back((uint16_t)i);
+            if (pat_at(i, k)) crow.push_back((uint16_t)i);
         h.lu_updates += (uint64_t)(lrow.size() - lbeg[k]) * (ucol.size() - ubeg[k]);
     }
     lbeg[n] = (uint32_t)lrow.size();
     ubeg[n] = (uint32_t)ucol.size();
     cbeg[n] = (uint32_t)crow.size();
+    std::vector<uint32_t> pat((size_t)n * 8, 0u);
+    std::vector<uint16_t> lcnt(n, 0);
+    for (uint32_t i = 0; i < n; ++i)
+        for (uint32_t j = 0; j < n; ++j)
+            if (pat_at(i, j)) {
+                pat[(size_t)i * 8 + (j >> 5)] |= 1u << (j & 31);
+                if (i > j) lcnt[j]++;
+            }
     h.fun_terms = (uint32_t)fent.size();
     h.jac_terms = (uint32_t)jent.size();
     h.l_entries = (uint32_t)lrow.size();
@@ -117,6 +125,8 @@ bool coop_image(const Model &m, std::vector<uint8_t> *out) {
     place(&h.off_ucol, ucol.size() * 2);
     place(&h.off_cbeg, cbeg.size() * 4);
     place(&h.off_crow, crow.size() * 2);
+    place(&h.off_pat, pat.size() * 4);
+    place(&h.off_lcnt, lcnt.size() * 2);
     if (off > 0xffffffffu) return false;
     h.bytes = (uint32_t)off;
     out->assign(off, 0);
@@ -139,6 +149,8 @@ bool coop_image(const Model &m, std::vector<uint8_t> *out) {
     put(h.off_ucol, ucol.data(), ucol.size() * 2);
     put(h.off_cbeg, cbeg.data(), cbeg.size() * 4);
     put(h.off_crow, crow.data(), crow.size() * 2);
+    put(h.off_pat, pat.data(), pat.size() * 4);
+    put(h.off_lcnt, lcnt.data(), lcnt.size() * 2);
     return true;
 }
 

@@ -8,8 +8,8 @@
 //
 // Precision 0: FP64 throughout, the same bits as the reference's solver (each
 // element sees the reference's operations in the reference's order; see
-// coop.h). The dense LU lives in per-CTA global scratch (L2-resident), with a
-// transposed copy of the factors for coalesced column reads in the solves.
+// coop.h). The dense LU lives in per-CTA global scratch (L2-resident); the
+// pattern bitmask, vectors and rates live in shared memory.
 // Precision 2 (mixed): FP64 RHS, Jacobian, residual, state and control; the
 // LU and the triangular solves in FP32 with the dense LU in shared memory;
 // each stage solve refined with FP64 residual sweeps.
@@ -72,7 +72,8 @@ struct CoopCell {
     double *y, *ytmp, *fcn, *src, *qv, *rb, *xv, *K, *kr, *rate, *red;
     float *x32;
     Cf *a;          // dense LU [n][ld]
-    Cf *tr;         // FP64: transposed factors [n][ld] (column k of L and U at row k)
+    const uint32_t *pat;    // shared: filled pattern, 8 words per row
+    const uint16_t *lcnt;   // shared: rows below the diagonal per column
     double *js;     // mixed: Jacobian entries (a = -J) in FP64
     // replicated scalar state (kin_solver.h:189-345)
     double t, h, seg_end, applied, duration, period, first, count, steps, rejects, pulses, failed;
@@ -81,6 +82,7 @@ struct CoopCell {
     bool pending, reject_last, reject_more;
 
     __device__ __forceinline__ void sync() const { __syncthreads(); }
+    __device__ __forceinline__ bool bit(uint32_t i, uint32_t j) const { return (pat[i * 8u + (j >> 5)] >> (j & 31u)) & 1u; }
 
     __device__ void load(const DevArgs &A, uint32_t cell) {
         const uint32_t p = A.padded;
@@ -208,92 +210,117 @@ struct CoopCell {
     }
 
     // In place: a -> L\U of (I ghinv - J), diagonal holding 1/U(k,k); pivot by
-    // pivot (kin_solver.h:97-113 applies the same updates row by row).
+    // pivot (kin_solver.h:97-113 applies the same updates row by row). Rows and
+    // columns are walked densely; the pattern bits select the elements the
+    // reference updates.
     __device__ void factor(Cf ghinv) {
         for (uint32_t k = 0; k < n; ++k) {
-            const uint32_t lb = tb.lbeg[k], nl = tb.lbeg[k + 1] - lb;
-            const uint32_t ub = tb.ubeg[k], nu = tb.ubeg[k + 1] - ub;
+            const uint32_t nl = lcnt[k];
             const Cf inv = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
             // L column k: l_i = a[i][k] / U(k,k)
-            for (uint32_t li = tid; li < nl; li += NT) {
-                const uint32_t i = tb.lrow[lb + li];
-                const Cf l = a[(size_t)i * ld + k] * inv;
-                a[(size_t)i * ld + k] = l;
-                if constexpr (!kMixed) tr[(size_t)k * ld + i] = l;
-            }
+            for (uint32_t i = k + 1 + tid; i < n; i += NT)
+                if (bit(i, k)) a[(size_t)i * ld + k] = a[(size_t)i * ld + k] * inv;
             if (nl) sync();
-            if (tid == 0) {
-                a[(size_t)k * ld + k] = inv;
-                if constexpr (!kMixed) tr[(size_t)k * ld + k] = inv;
-            }
-            // pivot row k (final) cached per lane; rows of L(k) updated warp by warp
+            if (tid == 0) a[(size_t)k * ld + k] = inv;
+            if (nl == 0) continue;   // nothing below the pivot: the next pivot reads none of this pivot's writes
+            // pivot row k (final) cached per lane: columns k+1+lane+32c in the pattern
+            const uint32_t width = n - 1 - k, chunks = (width + 31) / 32;
             Cf pv[kCoopMaxCols];
-            uint32_t cj[kCoopMaxCols];
+            uint32_t live = 0;
 #pragma unroll
             for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
-                const uint32_t uj = lane + 32u * c;
-                cj[c] = uj < nu ? tb.ucol[ub + uj] : 0u;
-                pv[c] = uj < nu ? a[(size_t)k * ld + cj[c]] : (Cf)0.0;
-            }
-            if constexpr (!kMixed) {
-                if (warp == 0) {
-#pragma unroll
-                    for (uint32_t c = 0; c < kCoopMaxCols; ++c)
-                        if (lane + 32u * c < nu) tr[(size_t)cj[c] * ld + k] = pv[c];
+                const uint32_t j = k + 1 + lane + 32u * c;
+                const bool on = c < chunks && j < n && bit(k, j);
+                pv[c] = (Cf)0.0;
+                if (on) {
+                    pv[c] = a[(size_t)k * ld + j];
+                    live |= 1u << c;
                 }
             }
-            if (nl == 0) continue;   // nothing below the pivot: the next pivot reads none of this pivot's writes
-            for (uint32_t li = warp; li < nl; li += W) {
-                const uint32_t i = tb.lrow[lb + li];
+            for (uint32_t i = k + 1 + warp; i < n; i += W) {
+                if (!bit(i, k)) continue;   // same for the whole warp
                 Cf *row = a + (size_t)i * ld;
                 const Cf l = row[k];
 #pragma unroll
-                for (uint32_t c = 0; c < kCoopMaxCols; ++c)
-                    if (lane + 32u * c < nu) row[cj[c]] = sgb_fma(-l, pv[c], row[cj[c]]);
+                for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
+                    const uint32_t j = k + 1 + lane + 32u * c;
+                    if ((live >> c) & 1u) row[j] = sgb_fma(-l, pv[c], row[j]);
+                }
             }
             sync();
         }
         sync();
     }
 
-    // x = (LU)^-1 x in place, column-oriented (the reference's row order per element);
-    // out receives the result (it may alias nothing else).
+    // x = (LU)^-1 x in place, in 32-column blocks. Forward (unit L): a warp
+    // solves the diagonal block with shuffles, then every row below takes the
+    // block's updates in ascending column order. Backward (U, diagonal holding
+    // 1/U(k,k)): blocks from the last; rows above take the block's updates in
+    // descending column order; a row's diagonal scaling follows its last update.
     template <class V>
-    __device__ void solve(V *x, V *out) {
-        const Cf *f = kMixed ? a : tr;   // mixed: columns of a (odd stride: conflict-free); FP64: rows of tr
-        for (uint32_t k = 0; k < n; ++k) {
-            const uint32_t lb = tb.lbeg[k], nl = tb.lbeg[k + 1] - lb;
-            if (nl == 0) continue;
-            const V xk = x[k];
-            for (uint32_t li = tid; li < nl; li += NT) {
-                const uint32_t i = tb.lrow[lb + li];
-                const V lik = kMixed ? (V)f[(size_t)i * ld + k] : (V)f[(size_t)k * ld + i];
-                x[i] = sgb_fma(-lik, xk, x[i]);
+    __device__ void solve(V *x) {
+        const uint32_t nb = (n + 31) / 32;
+        for (uint32_t b = 0; b < nb; ++b) {
+            const uint32_t kb = b * 32;
+            if (warp == 0) {
+                const uint32_t i = kb + lane;
+                V xi = i < n ? x[i] : (V)0.0;
+                const Cf *row = a + (size_t)(i < n ? i : 0) * ld;
+#pragma unroll 8
+                for (uint32_t kk = 0; kk < 32; ++kk) {
+                    const uint32_t k = kb + kk;
+                    const V xk = __shfl_sync(0xffffffffu, xi, kk);
+                    if (k < n && i > k && i < n && bit(i, k)) xi = sgb_fma(-(V)row[k < n ? k : 0], xk, xi);
+                }
+                if (i < n) x[i] = xi;
+            }
+            sync();
+            const uint32_t kend = kb + 32 < n ? kb + 32 : n;
+            for (uint32_t i = kend + tid; i < n; i += NT) {
+                const Cf *row = a + (size_t)i * ld;
+                V xi = x[i];
+                for (uint32_t k = kb; k < kend; ++k)
+                    if (bit(i, k)) xi = sgb_fma(-(V)row[k], x[k], xi);
+                x[i] = xi;
             }
             sync();
         }
-        for (uint32_t k = n; k-- > 0;) {
-            const V xk = x[k] * (V)f[(size_t)k * ld + k];
-            if (tid == 0) out[k] = xk;
-            const uint32_t cb = tb.cbeg[k], nc = tb.cbeg[k + 1] - cb;
-            if (nc == 0) continue;
-            for (uint32_t ci = tid; ci < nc; ci += NT) {
-                const uint32_t i = tb.crow[cb + ci];
-                const V uik = kMixed ? (V)f[(size_t)i * ld + k] : (V)f[(size_t)k * ld + i];
-                x[i] = sgb_fma(-uik, xk, x[i]);
+        for (uint32_t b = nb; b-- > 0;) {
+            const uint32_t kb = b * 32;
+            const uint32_t kend = kb + 32 < n ? kb + 32 : n;
+            if (warp == 0) {
+                const uint32_t i = kb + lane;
+                V xi = i < n ? x[i] : (V)0.0;
+                const Cf *row = a + (size_t)(i < n ? i : 0) * ld;
+#pragma unroll 8
+                for (uint32_t kk = 32; kk-- > 0;) {
+                    const uint32_t k = kb + kk;
+                    const uint32_t kc = k < n ? k : 0;
+                    if (k < n && lane == kk) xi = xi * (V)row[kc];   // row k: all its updates are in
+                    const V xk = __shfl_sync(0xffffffffu, xi, kk);
+                    if (k < n && i < k && bit(i, k)) xi = sgb_fma(-(V)row[kc], xk, xi);
+                }
+                if (i < n) x[i] = xi;
+            }
+            sync();
+            for (uint32_t i = tid; i < kb; i += NT) {
+                const Cf *row = a + (size_t)i * ld;
+                V xi = x[i];
+                for (uint32_t k = kend; k-- > kb;)
+                    if (bit(i, k)) xi = sgb_fma(-(V)row[k], x[k], xi);
+                x[i] = xi;
             }
             sync();
         }
-        sync();
     }
 
     // Mixed: out = W^-1 rb by the FP32 LU, then `sweeps` FP64-residual refinement sweeps.
     __device__ void solve_refined(const DevArgs &A, double ghinv, double *out) {
-        float *xs = x32, *xo = x32 + kCoopMaxSpecies;
+        float *xs = x32;
         for (uint32_t s = tid; s < n; s += NT) xs[s] = (float)rb[s];
         sync();
-        solve(xs, xo);
-        for (uint32_t s = tid; s < n; s += NT) out[s] = (double)xo[s];
+        solve(xs);
+        for (uint32_t s = tid; s < n; s += NT) out[s] = (double)xs[s];
         sync();
         for (uint32_t sw = 0; sw < A.ir_sweeps; ++sw) {
             for (uint32_t i = tid; i < n; i += NT) {
@@ -302,8 +329,8 @@ struct CoopCell {
                 xs[i] = (float)(rb[i] - w);
             }
             sync();
-            solve(xs, xo);
-            for (uint32_t s = tid; s < n; s += NT) out[s] = out[s] + (double)xo[s];
+            solve(xs);
+            for (uint32_t s = tid; s < n; s += NT) out[s] = out[s] + (double)xs[s];
             sync();
         }
     }
@@ -363,9 +390,7 @@ struct CoopCell {
             if constexpr (kMixed) {
                 solve_refined(A, ghinv, Ks);
             } else {
-                solve(Ks, xv);
-                for (uint32_t s = tid; s < n; s += NT) Ks[s] = xv[s];
-                sync();
+                solve(Ks);
             }
         }
 
@@ -451,16 +476,25 @@ __global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant_
     C.rate = C.kr + C.R;
     C.red = C.rate + C.R;
     C.x32 = (float *)(sm + coop_smem_doubles(n, C.R));
+    uint32_t *pat_s = (uint32_t *)(C.x32 + kCoopMaxSpecies);
+    uint16_t *lcnt_s = (uint16_t *)(pat_s + (size_t)n * 8);
+    {   // stage the pattern once per CTA
+        const uint32_t *pg = (const uint32_t *)((const unsigned char *)A.tables + C.tb.h->off_pat);
+        const uint16_t *lg = (const uint16_t *)((const unsigned char *)A.tables + C.tb.h->off_lcnt);
+        for (uint32_t q = threadIdx.x; q < n * 8; q += blockDim.x) pat_s[q] = pg[q];
+        for (uint32_t q = threadIdx.x; q < n; q += blockDim.x) lcnt_s[q] = lg[q];
+    }
+    C.pat = pat_s;
+    C.lcnt = lcnt_s;
     double *g = scratch + (size_t)blockIdx.x * stride;
     if constexpr (PREC == 2) {
-        C.a = (typename CoopCell<PREC>::Cf *)(C.x32 + 2 * kCoopMaxSpecies);
-        C.tr = nullptr;
+        C.a = (typename CoopCell<PREC>::Cf *)(lcnt_s + ((n + 7) / 8) * 8);   // 16-byte aligned
         C.js = g;
     } else {
         C.a = (typename CoopCell<PREC>::Cf *)g;
-        C.tr = (typename CoopCell<PREC>::Cf *)(g + (size_t)n * C.ld);
         C.js = nullptr;
     }
+    __syncthreads();
     for (;;) {
         if (threadIdx.x == 0) cell_s = atomicAdd(A.cursor, 1u);
         __syncthreads();
@@ -490,14 +524,15 @@ struct CoopModule {
 };
 CoopModule cm;
 
+// Shared memory: doubles, x32 (256 floats), pattern (n x 8 words), lcnt (n u16, padded), mixed: a (n x ld floats).
 size_t coop_smem_bytes(int prec, const CoopMech &h) {
-    size_t b = (size_t)coop_smem_doubles(h.n, h.R) * 8;
-    if (prec == 2) b += 2 * kCoopMaxSpecies * 4 + (size_t)h.n * h.ld * 4;
+    size_t b = (size_t)coop_smem_doubles(h.n, h.R) * 8 + kCoopMaxSpecies * 4 + (size_t)h.n * 32 + ((h.n + 7) / 8) * 16;
+    if (prec == 2) b += (size_t)h.n * h.ld * 4;
     return b;
 }
 
 size_t coop_scratch_doubles(int prec, const CoopMech &h) {
-    size_t d = prec == 2 ? (size_t)h.nj : 2 * (size_t)h.n * h.ld;
+    size_t d = prec == 2 ? (size_t)h.nj : (size_t)h.n * h.ld;
     return (d + 31) / 32 * 32;   // 256-byte aligned per CTA
 }
 
