@@ -61,8 +61,9 @@ def parse():
     ap.add_argument("--requests", type=int, default=48, help="config5: requests in the served sample")
     ap.add_argument("--fp64-cells", type=int, default=1216,
                     help="config4: cells of the FP64 comparison sample (the first cells of the workload)")
-    ap.add_argument("--profile-case", choices=["f64", "mixed", "f32"], default=None,
-                    help="one queue-kernel advance of --cells x --duration at this precision, then exit (ncu captures)")
+    ap.add_argument("--profile-case", choices=["f64", "mixed", "f32", "coop-f64", "coop-mixed"], default=None,
+                    help="one advance of --cells x --duration at this precision, then exit (ncu captures): the "
+                         "queue kernel on the shipped mechanism, or the cooperative kernel on the 200-species one")
     return ap.parse_args()
 
 
@@ -703,6 +704,18 @@ def run_config5(args):
 def run_profile_case(args):
     """One advance on cuda:0 for an ncu capture: the persistent queue kernel, default tuning."""
     import simstack_gb300 as sg
+
+    if args.profile_case.startswith("coop"):
+        prec = 0 if args.profile_case == "coop-f64" else 2
+        pm = sg.Model.synthetic(seed=args.seed, species=200, reactions=1200, bimolecular=0.7, products=1)
+        z = sg.synthetic_cells(pm, args.cells, seed=args.seed + 1)
+        mod = sg.Module(0, 2 * z.nbytes + (64 << 20))
+        mod.coop_set_mech(pm, sg.method("rodas3"), sg.control(rtol=1e-4, atol=1e-12, max_steps=200000))
+        ms = mod.coop_integrate(z, args.duration, precision=prec)
+        steps = float(z["steps"][:args.cells].sum() + z["rejects"][:args.cells].sum())
+        print(json.dumps({"case": args.profile_case, "cells": args.cells, "duration_s": args.duration, "kernel_ms": ms,
+                          "cell_steps": steps}))
+        return
 
     prec = {"f64": 0, "f32": 1, "mixed": 2}[args.profile_case]
     mod = sg.Module(0, 2 * sg.ZoneBlock(17, 44, args.cells).nbytes + (64 << 20))

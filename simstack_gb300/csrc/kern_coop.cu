@@ -262,25 +262,27 @@ struct CoopCell {
         const uint32_t nb = (n + 31) / 32;
         for (uint32_t b = 0; b < nb; ++b) {
             const uint32_t kb = b * 32;
+            const uint32_t kend = kb + 32 < n ? kb + 32 : n;
             if (warp == 0) {
                 const uint32_t i = kb + lane;
                 V xi = i < n ? x[i] : (V)0.0;
                 const Cf *row = a + (size_t)(i < n ? i : 0) * ld;
+                // this row's pattern bits for the block's columns, below the diagonal only
+                const uint32_t w = i < n ? pat[i * 8u + b] & ((1u << lane) - 1u) : 0u;
 #pragma unroll 8
                 for (uint32_t kk = 0; kk < 32; ++kk) {
-                    const uint32_t k = kb + kk;
                     const V xk = __shfl_sync(0xffffffffu, xi, kk);
-                    if (k < n && i > k && i < n && bit(i, k)) xi = sgb_fma(-(V)row[k < n ? k : 0], xk, xi);
+                    if ((w >> kk) & 1u) xi = sgb_fma(-(V)row[kb + kk], xk, xi);
                 }
                 if (i < n) x[i] = xi;
             }
             sync();
-            const uint32_t kend = kb + 32 < n ? kb + 32 : n;
             for (uint32_t i = kend + tid; i < n; i += NT) {
                 const Cf *row = a + (size_t)i * ld;
+                const uint32_t w = pat[i * 8u + b];
                 V xi = x[i];
                 for (uint32_t k = kb; k < kend; ++k)
-                    if (bit(i, k)) xi = sgb_fma(-(V)row[k], x[k], xi);
+                    if ((w >> (k - kb)) & 1u) xi = sgb_fma(-(V)row[k], x[k], xi);
                 x[i] = xi;
             }
             sync();
@@ -292,22 +294,24 @@ struct CoopCell {
                 const uint32_t i = kb + lane;
                 V xi = i < n ? x[i] : (V)0.0;
                 const Cf *row = a + (size_t)(i < n ? i : 0) * ld;
+                // this row's pattern bits for the block's columns, above the diagonal only (columns < n)
+                const uint32_t w = i < n ? pat[i * 8u + b] & ~((2u << lane) - 1u) : 0u;
+                const V d = i < n ? (V)row[i] : (V)0.0;   // 1/U(i,i)
 #pragma unroll 8
                 for (uint32_t kk = 32; kk-- > 0;) {
-                    const uint32_t k = kb + kk;
-                    const uint32_t kc = k < n ? k : 0;
-                    if (k < n && lane == kk) xi = xi * (V)row[kc];   // row k: all its updates are in
+                    if (lane == kk) xi = xi * d;   // row kb+kk: all its updates are in
                     const V xk = __shfl_sync(0xffffffffu, xi, kk);
-                    if (k < n && i < k && bit(i, k)) xi = sgb_fma(-(V)row[kc], xk, xi);
+                    if ((w >> kk) & 1u) xi = sgb_fma(-(V)row[kb + kk], xk, xi);
                 }
                 if (i < n) x[i] = xi;
             }
             sync();
             for (uint32_t i = tid; i < kb; i += NT) {
                 const Cf *row = a + (size_t)i * ld;
+                const uint32_t w = pat[i * 8u + b];
                 V xi = x[i];
                 for (uint32_t k = kend; k-- > kb;)
-                    if (bit(i, k)) xi = sgb_fma(-(V)row[k], x[k], xi);
+                    if ((w >> (k - kb)) & 1u) xi = sgb_fma(-(V)row[k], x[k], xi);
                 x[i] = xi;
             }
             sync();
