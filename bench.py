@@ -59,6 +59,8 @@ def parse():
                          "config4: 200-species / 1,200-reaction synthetic mechanism, one CTA per cell; "
                          "config5: served requests (Poisson arrivals) with film advection, p50/p99 latency")
     ap.add_argument("--requests", type=int, default=48, help="config5: requests in the served sample")
+    ap.add_argument("--mixed-variant", type=int, choices=[0, 1], default=None,
+                    help="--profile-case mixed: 0 = FP64 state with refinement, 1 = double-float state (default)")
     ap.add_argument("--fp64-cells", type=int, default=1216,
                     help="config4: cells of the FP64 comparison sample (the first cells of the workload)")
     ap.add_argument("--profile-case", choices=["f64", "mixed", "f32", "coop-f64", "coop-mixed"], default=None,
@@ -189,10 +191,11 @@ def flops_per_step(model) -> dict:
 
 
 # DRAM bytes (read + write) per attempted cell-step of the queue kernels, from one ncu capture each
-# (262,144 cells x 0.5 s, `bench.py --profile-case f64|mixed`; summaries in
-# profiles/kin_queue_cta_{f64,mixed}_air_262144x0.5s.txt). Nearly all of it is local-memory spill
-# traffic, which grows with the cell-steps a launch executes; the bench scales it to its own launch.
-DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 8624.7}
+# (262,144 cells x 0.5 s, `bench.py --profile-case f64|mixed`, default tuning; summaries in
+# profiles/kin_queue_cta_f64_air_262144x0.5s.txt and profiles/kin_queue_cta_mixed_df_air_262144x0.5s.txt).
+# Nearly all of it is local-memory spill traffic, which grows with the cell-steps a launch executes;
+# the bench scales it to its own launch.
+DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 1916.1}
 
 
 def hbm_bytes_per_cell(n: int, R: int) -> int:
@@ -719,6 +722,8 @@ def run_profile_case(args):
 
     prec = {"f64": 0, "f32": 1, "mixed": 2}[args.profile_case]
     mod = sg.Module(0, 2 * sg.ZoneBlock(17, 44, args.cells).nbytes + (64 << 20))
+    if args.mixed_variant is not None:
+        mod.set_mixed_variant(args.mixed_variant)
     ctl = sg.control() if prec != 1 else sg.control(rtol=1e-3, atol=1e8, max_steps=20000)
     mod.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), ctl)
     z = sg.air_cells(args.cells, seed=args.seed)

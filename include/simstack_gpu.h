@@ -189,11 +189,12 @@ SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_
 
 /* Launch tuning. kind: 0 static one-cell-per-thread, 1 persistent queue
  * (warp-synchronous), 2 persistent queue with the CTA's warps stepping
- * together (default). block = threads per CTA (multiple of 32; <= 128, or
- * 256 with variant 2), chunk = resident CTAs per SM for the queue kernels
- * (0: as many as fit), variant = compiled register-budget variant (0: up to
- * 255 registers at 128 threads, 1: 128 registers, 2: 255 registers at 256
- * threads, kind 2 only).
+ * together (default). block = threads per CTA (multiple of 32; <= 128, 256
+ * with variant 2, 512 with variant 3), chunk = resident CTAs per SM for the
+ * queue kernels (0: as many as fit), variant = compiled register-budget
+ * variant (0: up to 255 registers at 128 threads, 1: 128 registers, 2: 255
+ * registers at 256 threads, kind 2 only; 3: 128 registers at 512 threads,
+ * kind 2 only).
  * gpu_kin_autotune times candidates on the given launch (which it advances
  * repeatedly on a scratch copy it restores) and keeps the fastest. */
 typedef struct GpuKinTuning {
@@ -266,6 +267,10 @@ SGB_API int32_t gpu_kin_coop_set_mech(const KinModelHandle *model, const KinMeth
 SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *launch, float *kernel_ms);
 /* out[8]: n, R, LU non-zeros, Jacobian entries, L entries, U entries, LU updates, image bytes. */
 SGB_API int32_t gpu_kin_coop_info(uint64_t *out);
+/* Launch shape of the cooperative kernels per precision (0 or 2): threads per CTA (64..512,
+ * multiple of 32) and resident CTAs per SM (1..2; capped by occupancy). Defaults: FP64 256 x 2,
+ * mixed 512 x 1 (its FP32 LU fills one SM's shared memory). */
+SGB_API int32_t gpu_kin_coop_set_shape(uint32_t precision, uint32_t block, uint32_t ctas_per_sm);
 /* Refinement sweeps per stage solve of the mixed cooperative path (1..4, default 1). */
 SGB_API int32_t gpu_kin_coop_set_refinement(uint32_t sweeps);
 

@@ -401,9 +401,9 @@ SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_
 }
 
 SGB_API int32_t gpu_kin_set_tuning(const GpuKinTuning *t) {
-    if (!t || t->kind > 2 || t->block == 0 || (t->block & 31) || t->variant > 2 || t->chunk > 64) return (int32_t)cudaErrorInvalidValue;
-    const uint32_t max_block = t->variant == 2 ? 256u : 128u;   // the variant's __launch_bounds__
-    if (t->block > max_block || (t->variant == 2 && t->kind != 2)) return (int32_t)cudaErrorInvalidValue;
+    if (!t || t->kind > 2 || t->block == 0 || (t->block & 31) || t->variant > 3 || t->chunk > 64) return (int32_t)cudaErrorInvalidValue;
+    const uint32_t max_block = t->variant == 3 ? 512u : t->variant == 2 ? 256u : 128u;   // the variant's __launch_bounds__
+    if (t->block > max_block || (t->variant >= 2 && t->kind != 2)) return (int32_t)cudaErrorInvalidValue;
     for (int p = 0; p < 3; ++p) g.tuning[p] = *t;
     return 0;
 }
@@ -442,7 +442,7 @@ SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuK
     struct Cand { uint32_t block, variant, ctas; };
     const Cand cands[] = {{32, 0, 0}, {64, 0, 0}, {128, 0, 0}, {64, 1, 0}, {128, 1, 0},
                           {128, 0, 1}, {64, 0, 2}, {64, 0, 3}, {128, 1, 2}, {128, 1, 3}};
-    const Cand sync_cands[] = {{256, 2, 1}, {128, 0, 2}, {128, 0, 1}, {128, 1, 3}, {128, 1, 4}};
+    const Cand sync_cands[] = {{256, 2, 1}, {128, 0, 2}, {128, 0, 1}, {128, 1, 3}, {128, 1, 4}, {512, 3, 1}};
     GpuKinTuning winner = g.tuning[launch->precision];
     winner.ms = 1e30f;
     const Cand *list = kind == 2 ? sync_cands : cands;

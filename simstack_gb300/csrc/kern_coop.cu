@@ -525,8 +525,12 @@ struct CoopModule {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t ir_sweeps = 1;
     float last_ms = 0.0f;
+    uint32_t block[3] = {256, 0, 512};    // threads per CTA by precision (0 FP64, 2 mixed)
+    uint32_t ctas[3] = {2, 0, 1};         // resident CTAs per SM by precision
+    int sms = 0;
 };
 CoopModule cm;
+constexpr uint32_t kCoopMaxCtasPerSm = 2;   // scratch slots per SM
 
 // Shared memory: doubles, x32 (256 floats), pattern (n x 8 words), lcnt (n u16, padded), mixed: a (n x ld floats).
 size_t coop_smem_bytes(int prec, const CoopMech &h) {
@@ -574,7 +578,7 @@ SGB_API int32_t gpu_kin_coop_set_mech(const KinModelHandle *model, const KinMeth
     // scratch for the larger of the two precisions' needs, one slot per resident CTA (one CTA per SM)
     const size_t per = coop_scratch_doubles(0, h) > coop_scratch_doubles(2, h) ? coop_scratch_doubles(0, h)
                                                                               : coop_scratch_doubles(2, h);
-    const size_t need = per * 8 * (size_t)sms;
+    const size_t need = per * 8 * (size_t)sms * kCoopMaxCtasPerSm;
     if (e == cudaSuccess && need > cm.scratch_bytes) {
         if (cm.d_scratch) cudaFree(cm.d_scratch);
         cm.d_scratch = nullptr;
@@ -587,6 +591,7 @@ SGB_API int32_t gpu_kin_coop_set_mech(const KinModelHandle *model, const KinMeth
     if (e != cudaSuccess) return (int32_t)e;
     cm.image.swap(img);
     cm.head = h;
+    cm.sms = sms;
     cm.method = *method;
     cm.control = *control;
     cm.ready = true;
@@ -640,13 +645,18 @@ SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *L, float *kernel_ms) {
     const size_t smem = coop_smem_bytes(prec, cm.head);
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int32_t)e;
-    const uint32_t grid = (uint32_t)sms < A.lanes ? (uint32_t)sms : A.lanes;
+    int fit = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, (int)cm.block[prec], smem);
+    if (e != cudaSuccess) return (int32_t)e;
+    const uint32_t per_sm = (uint32_t)(fit < 1 ? 1 : fit) < cm.ctas[prec] ? (uint32_t)(fit < 1 ? 1 : fit) : cm.ctas[prec];
+    const uint32_t resident = per_sm * (uint32_t)sms;
+    const uint32_t grid = resident < A.lanes ? resident : A.lanes;
     const uint64_t stride = coop_scratch_doubles(prec, cm.head);
     cudaStream_t s = (cudaStream_t)gpu_stream();
     e = cudaMemsetAsync(cm.d_header, 0, 256, s);
     if (e == cudaSuccess) e = cudaEventRecord(cm.ev0, s);
     if (e != cudaSuccess) return (int32_t)e;
-    fn<<<grid, 512, smem, s>>>(A, cm.d_scratch, stride);
+    fn<<<grid, cm.block[prec], smem, s>>>(A, cm.d_scratch, stride);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaEventRecord(cm.ev1, s);
     if (e == cudaSuccess) e = cudaEventSynchronize(cm.ev1);
@@ -665,6 +675,15 @@ SGB_API int32_t gpu_kin_coop_info(uint64_t *out8) {
     const CoopMech &h = cm.head;
     out8[0] = h.n; out8[1] = h.R; out8[2] = h.nnz; out8[3] = h.nj;
     out8[4] = h.l_entries; out8[5] = h.u_entries; out8[6] = h.lu_updates; out8[7] = h.bytes;
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_coop_set_shape(uint32_t precision, uint32_t block, uint32_t ctas_per_sm) {
+    if ((precision != 0 && precision != 2) || block < 64 || block > 512 || (block & 31) || ctas_per_sm < 1 ||
+        ctas_per_sm > kCoopMaxCtasPerSm)
+        return (int32_t)cudaErrorInvalidValue;
+    cm.block[precision] = block;
+    cm.ctas[precision] = ctas_per_sm;
     return 0;
 }
 

@@ -23,6 +23,7 @@ template <int V> struct Budget;
 template <> struct Budget<0> { static constexpr int kThreads = 128, kMinBlocks = 1; };
 template <> struct Budget<1> { static constexpr int kThreads = 128, kMinBlocks = 4; };
 template <> struct Budget<2> { static constexpr int kThreads = 256, kMinBlocks = 1; };
+template <> struct Budget<3> { static constexpr int kThreads = 512, kMinBlocks = 1; };   // 128 registers
 
 // Both kernels keep every lane of a warp in the loop until the whole warp is
 // out of work, and vote (__any_sync) once per iteration: the vote is a
@@ -144,8 +145,10 @@ struct Shape {
 // kVariants: how many register-budget variants are instantiated (1: variant 0 only).
 template <class Ops, class M, int PREC, int kVariants>
 void (*kernel_for(uint32_t kind, uint32_t variant))(DevArgs) {
-    if (kind == 2) {   // CTA-synchronous queue: 128 threads (variant 0) or 256 threads, one CTA per SM (variant 2)
+    if (kind == 2) {   // CTA-synchronous queue: 128 threads (variants 0, 1), 256 threads (2) or 512 threads (3)
+        if (kVariants > 1 && variant == 1) return kin_queue_cta_kernel<Ops, M, PREC, (kVariants > 1 ? 1 : 0)>;
         if (kVariants > 1 && variant == 2) return kin_queue_cta_kernel<Ops, M, PREC, (kVariants > 1 ? 2 : 0)>;
+        if (kVariants > 1 && variant == 3) return kin_queue_cta_kernel<Ops, M, PREC, (kVariants > 1 ? 3 : 0)>;
         return kin_queue_cta_kernel<Ops, M, PREC, 0>;
     }
     if (kVariants > 1 && variant == 1)
