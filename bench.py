@@ -488,6 +488,9 @@ def run_ours(args):
 # steps from ~150 to ~2,700 per cell over 60 s on these initial states (p50 ~280),
 # measured on the oracle (64-cell sample, seed 3).
 CONFIG3_P0 = 1e-2
+# Straggler hand-off budget: cells past this many step attempts in one advance (about 2x the p99 of
+# this workload's step counts) finish on the cooperative kernel.
+CONFIG3_BUDGET = 1200
 
 
 def run_config3(args):
@@ -504,9 +507,11 @@ def run_config3(args):
     work = mod.alloc(z.nbytes)
     launch = z.launch(work, 0, duration)
     results = {}
+    zf = None
     for prec in (0, 2):
         launch.precision = prec
-        for kind in (0, 2):
+        for kind, budget in ((0, 0), (2, 0), (2, CONFIG3_BUDGET)):
+            mod.set_straggler_budget(budget)
             sg.check(L.gpu_copy_on_device(work, pristine, z.nbytes), "copy")
             t = mod.autotune(launch, kind=kind)
             times = []
@@ -516,13 +521,30 @@ def run_config3(args):
                 if it >= args.warmup:
                     times.append(ms)
             ms = float(np.mean(times))
-            results[f"{'f64' if prec == 0 else 'mixed'}_{'static' if kind == 0 else 'queue'}"] = {
-                "ms": ms, "value": cells / (ms * 1e-3), "tuning": {"block": t.block, "variant": t.variant, "ctas_per_sm": t.chunk}}
-    zc = z.copy()
-    mod.download(zc, work)
-    steps = zc["steps"][:cells]
-    line = {"metric": "cell-integrations/s", "value": results["mixed_queue"]["value"], "unit": "cell-integrations/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": results["mixed_queue"]["ms"],
+            key = f"{'f64' if prec == 0 else 'mixed'}_{'static' if kind == 0 else 'queue'}{'_handoff' if budget else ''}"
+            results[key] = {"ms": ms, "value": cells / (ms * 1e-3),
+                            "tuning": {"block": t.block, "variant": t.variant, "ctas_per_sm": t.chunk}}
+            if budget:
+                results[key]["parked_cells"] = mod.parked_cells()
+                results[key]["budget_attempts"] = budget
+            zo = z.copy()
+            mod.download(zo, work)
+            if prec == 0 and zf is None:
+                zf = zo
+            elif prec == 0:   # the hand-off keeps the FP64 bits
+                results[key]["same_bits_as_f64_static"] = bool(zo["y"].tobytes() == zf["y"].tobytes())
+            else:
+                b, a = zf["y"][:, :cells], zo["y"][:, :cells]
+                sig = b >= 1e-12 * b.sum(axis=0)
+                with np.errstate(all="ignore"):
+                    rel = (np.abs(a - b) / np.abs(b))[sig]
+                results[key]["rel_err_vs_fp64"] = {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99))}
+    mod.set_straggler_budget(0)
+    steps = zf["steps"][:cells]   # FP64 path: the oracle's step counts
+    best = min((k for k in results if k.startswith("mixed")), key=lambda k: results[k]["ms"])
+    line = {"metric": "cell-integrations/s", "value": results[best]["value"], "unit": "cell-integrations/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": results[best]["ms"],
+            "headline_kernel": best,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"uneven stiffness: shipped mechanism, {cells} cells x {duration:g} s, averaged discharge "
                                    f"source at P0 x 10^U[0,3] W/cm^3, P0 = {CONFIG3_P0:g}",
@@ -531,7 +553,9 @@ def run_config3(args):
                                         "p99": float(np.quantile(steps, 0.99)), "max": float(steps.max())},
             "kernels": results,
             "queue_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue"]["ms"],
-                                        "mixed": results["mixed_static"]["ms"] / results["mixed_queue"]["ms"]}}
+                                        "mixed": results["mixed_static"]["ms"] / results["mixed_queue"]["ms"]},
+            "handoff_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue_handoff"]["ms"],
+                                          "mixed": results["mixed_static"]["ms"] / results["mixed_queue_handoff"]["ms"]}}
     print(json.dumps(line))
 
 

@@ -215,6 +215,14 @@ SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps);
  * LU and solves, stage right-hand sides accumulated in double-float, almost no FP64 work per species
  * (only the scalar step controller stays FP64). Default 1. */
 SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant);
+/* Straggler hand-off (0 = off, the default): in one advance, a cell still stepping after
+ * `attempts` step attempts on its lane is parked and finished right after by the cooperative
+ * kernel (one CTA per cell, every thread sharing the cell's work), so a few very stiff cells
+ * no longer run alone on single lanes at the end of the launch. Precision 0 keeps the same
+ * bits; the double-float mixed path finishes parked cells on the cooperative mixed path. */
+SGB_API int32_t gpu_kin_set_straggler_budget(uint32_t attempts);
+/* Cells parked by the last advance that used the hand-off (waits for the module stream). */
+SGB_API int32_t gpu_kin_parked_cells(uint32_t *count);
 SGB_API uint32_t gpu_kin_get_mixed_variant(void);
 
 /* Measured instruction throughput of this device, operations per second (an

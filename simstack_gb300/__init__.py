@@ -157,6 +157,8 @@ def lib() -> C.CDLL:
             "gpu_kin_set_refinement": (i32, [u32]),
             "gpu_kin_set_mixed_variant": (i32, [u32]),
             "gpu_kin_get_mixed_variant": (u32, []),
+            "gpu_kin_set_straggler_budget": (i32, [u32]),
+            "gpu_kin_parked_cells": (i32, [C.POINTER(u32)]),
             "gpu_probe_throughput": (i32, [u32, C.POINTER(d)]),
             "gpu_stream": (vp, []),
             "gpu_copy_on_device": (i32, [vp, vp, u64]),
@@ -516,6 +518,15 @@ class Module:
 
     def mixed_variant(self) -> int:
         return int(lib().gpu_kin_get_mixed_variant())
+
+    def set_straggler_budget(self, attempts: int) -> None:
+        """Cells still stepping after `attempts` attempts are finished by the cooperative kernel (0 = off)."""
+        check(lib().gpu_kin_set_straggler_budget(attempts), "gpu_kin_set_straggler_budget")
+
+    def parked_cells(self) -> int:
+        c = C.c_uint32()
+        check(lib().gpu_kin_parked_cells(C.byref(c)), "gpu_kin_parked_cells")
+        return c.value
 
     # cooperative kernels (one CTA per cell): mechanisms beyond the KinMech tables
     def coop_set_mech(self, model: "Model", meth: KinMethod | None = None, ctl: KinControl | None = None) -> None:

@@ -1,5 +1,6 @@
 // Host side of the cooperative kernels: the wide-index mechanism image
-// (coop.h) built from a finalized Model's symbolic phase.
+// (coop.h) built from a finalized Model's symbolic phase or from a
+// reference-layout KinMech (the same pattern, slots and scatter lists).
 #include <string.h>
 
 #include "coop.h"
@@ -9,33 +10,95 @@ namespace sgb {
 
 namespace {
 uint32_t align16(size_t v) { return (uint32_t)((v + 15) / 16 * 16); }
+
+// What the image needs, from either source (a Model or a reference-layout KinMech).
+struct Desc {
+    uint32_t n = 0, R = 0, nnz = 0;
+    std::vector<std::vector<uint32_t>> reactants;                   // per reaction, equation order
+    std::vector<std::vector<std::pair<uint32_t, int32_t>>> net;     // per reaction, (species, change)
+    std::vector<std::vector<std::vector<uint32_t>>> jac_slot;       // [r][p][e] -> compact slot
+    std::vector<uint8_t> pattern;                                   // n x n after fill-in
+    std::vector<uint32_t> slot;                                     // n x n -> compact slot or ~0u
+};
+
+bool build_image(const Desc &d, std::vector<uint8_t> *out);
+
 }   // namespace
 
 bool coop_image(const Model &m, std::vector<uint8_t> *out) {
     if (!m.finalized) return false;
-    const Symbolic &S = m.sym;
-    const uint32_t n = m.n(), R = m.R();
+    Desc d;
+    d.n = m.n();
+    d.R = m.R();
+    d.nnz = m.sym.nnz;
+    for (const Reaction &rx : m.reactions) {
+        d.reactants.push_back(rx.reactants);
+        d.net.push_back(rx.net);
+        d.jac_slot.push_back(rx.jac_slot);
+    }
+    d.pattern = m.sym.pattern;
+    d.slot = m.sym.slot;
+    return build_image(d, out);
+}
+
+bool coop_image(const KinMech &k, std::vector<uint8_t> *out) {
+    Desc d;
+    d.n = k.species_count;
+    d.R = k.reaction_count;
+    d.nnz = k.nnz;
+    const uint32_t n = d.n;
+    if (n == 0 || n > KIN_MAX_SPECIES || d.R > KIN_MAX_REACTIONS) return false;
+    d.pattern.assign((size_t)n * n, 0);
+    d.slot.assign((size_t)n * n, ~0u);
+    auto put = [&](uint32_t i, uint32_t j, uint32_t s) {
+        d.pattern[(size_t)i * n + j] = 1;
+        d.slot[(size_t)i * n + j] = s;
+    };
+    for (uint32_t i = 0; i < n; ++i) {
+        put(i, i, k.diag[i]);
+        for (uint32_t e = k.lower_begin[i]; e < k.lower_begin[i + 1]; ++e) put(i, k.lower[e].col, k.lower[e].index);
+        for (uint32_t e = k.upper_begin[i]; e < k.upper_begin[i + 1]; ++e) put(i, k.upper[e].col, k.upper[e].index);
+    }
+    for (uint32_t r = 0; r < d.R; ++r) {
+        const KinReaction &rx = k.reactions[r];
+        std::vector<uint32_t> re;
+        for (uint32_t p = 0; p < rx.reactant_count; ++p) re.push_back(rx.reactant[p]);
+        std::vector<std::pair<uint32_t, int32_t>> nt;
+        for (uint32_t e = 0; e < rx.net_count; ++e) nt.push_back({rx.net_species[e], (int32_t)rx.net_coef[e]});
+        std::vector<std::vector<uint32_t>> js(rx.reactant_count, std::vector<uint32_t>(rx.net_count));
+        for (uint32_t p = 0; p < rx.reactant_count; ++p)
+            for (uint32_t e = 0; e < rx.net_count; ++e) js[p][e] = rx.jac_index[p][e];
+        d.reactants.push_back(re);
+        d.net.push_back(nt);
+        d.jac_slot.push_back(js);
+    }
+    return build_image(d, out);
+}
+
+namespace {
+
+bool build_image(const Desc &d, std::vector<uint8_t> *out) {
+    const uint32_t n = d.n, R = d.R;
     if (n == 0 || n > 256) return false;   // pattern rows are 256-bit masks
-    auto pat_at = [&](uint32_t i, uint32_t j) { return S.pattern[(size_t)i * n + j] != 0; };
+    auto pat_at = [&](uint32_t i, uint32_t j) { return d.pattern[(size_t)i * n + j] != 0; };
 
     CoopMech h;
     memset(&h, 0, sizeof(h));
     h.n = n;
     h.R = R;
     h.ld = n | 1u;
-    h.nnz = S.nnz;
+    h.nnz = d.nnz;
 
     std::vector<uint16_t> reac((size_t)R * 4, 0);
     for (uint32_t r = 0; r < R; ++r) {
-        const Reaction &rx = m.reactions[r];
-        if (rx.reactants.size() > 3) return false;
-        reac[(size_t)r * 4] = (uint16_t)rx.reactants.size();
-        for (size_t p = 0; p < rx.reactants.size(); ++p) reac[(size_t)r * 4 + 1 + p] = (uint16_t)rx.reactants[p];
+        if (d.reactants[r].size() > 3) return false;
+        reac[(size_t)r * 4] = (uint16_t)d.reactants[r].size();
+        for (size_t p = 0; p < d.reactants[r].size(); ++p) reac[(size_t)r * 4 + 1 + p] = (uint16_t)d.reactants[r][p];
     }
     // RHS terms per species, reactions ascending
     std::vector<std::vector<CoopTerm>> fs(n);
     for (uint32_t r = 0; r < R; ++r)
-        for (auto &e : m.reactions[r].net) fs[e.first].push_back({r, (float)e.second});
+        for (auto &e : d.net[r]) fs[e.first].push_back({r, (float)e.second});
     std::vector<uint32_t> fbeg(n + 1, 0);
     std::vector<CoopTerm> fent;
     for (uint32_t s = 0; s < n; ++s) {
@@ -44,17 +107,18 @@ bool coop_image(const Model &m, std::vector<uint8_t> *out) {
     }
     fbeg[n] = (uint32_t)fent.size();
     // Jacobian terms per compact slot, (r, p, e) ascending; entries = slots some reaction scatters into
-    std::vector<std::vector<CoopTerm>> js(S.nnz);
-    for (uint32_t r = 0; r < R; ++r) {
-        const Reaction &rx = m.reactions[r];
-        for (size_t p = 0; p < rx.reactants.size(); ++p)
-            for (size_t e = 0; e < rx.net.size(); ++e)
-                js[rx.jac_slot[p][e]].push_back({r | ((uint32_t)p << 24), (float)(-rx.net[e].second)});
-    }
-    std::vector<uint32_t> slot_row(S.nnz), slot_col(S.nnz);
+    std::vector<std::vector<CoopTerm>> js(d.nnz);
+    for (uint32_t r = 0; r < R; ++r)
+        for (size_t p = 0; p < d.reactants[r].size(); ++p)
+            for (size_t e = 0; e < d.net[r].size(); ++e) {
+                const uint32_t sl = d.jac_slot[r][p][e];
+                if (sl >= d.nnz) return false;
+                js[sl].push_back({r | ((uint32_t)p << 24), (float)(-d.net[r][e].second)});
+            }
+    std::vector<uint32_t> slot_row(d.nnz), slot_col(d.nnz);
     for (uint32_t i = 0; i < n; ++i)
         for (uint32_t j = 0; j < n; ++j) {
-            uint32_t s = S.slot[(size_t)i * n + j];
+            uint32_t s = d.slot[(size_t)i * n + j];
             if (s != ~0u) {
                 slot_row[s] = i;
                 slot_col[s] = j;
@@ -63,7 +127,7 @@ bool coop_image(const Model &m, std::vector<uint8_t> *out) {
     std::vector<uint32_t> jbeg, jpos, jrow(n + 1, 0);
     std::vector<uint16_t> jcol;
     std::vector<CoopTerm> jent;
-    for (uint32_t s = 0; s < S.nnz; ++s) {   // slots are row-major, so entries come out sorted by row
+    for (uint32_t s = 0; s < d.nnz; ++s) {   // slots are row-major, so entries come out sorted by row
         if (js[s].empty()) continue;
         jbeg.push_back((uint32_t)jent.size());
         jent.insert(jent.end(), js[s].begin(), js[s].end());
@@ -153,5 +217,7 @@ bool coop_image(const Model &m, std::vector<uint8_t> *out) {
     put(h.off_lcnt, lcnt.data(), lcnt.size() * 2);
     return true;
 }
+
+}   // namespace
 
 }   // namespace sgb

@@ -13,6 +13,9 @@
 #include "kin_table.cuh"
 #include "mech.h"
 #include "mech_tables.h"
+#include "coop.h"
+
+#include <vector>
 
 namespace sgb {
 cudaError_t launch_air_p0(const Shape &, const DevArgs &, cudaStream_t);
@@ -32,6 +35,10 @@ cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
 cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
 uint64_t air_ops_signature();
+size_t coop_smem_bytes_for(int prec, const CoopMech &h);
+size_t coop_scratch_doubles_for(int prec, const CoopMech &h);
+cudaError_t coop_resume_launch(int prec, const DevArgs &A, const CoopMech &head, double *scratch, uint32_t grid,
+                               uint32_t block, cudaStream_t s);
 cudaError_t run_probe(uint32_t kind, int sms, cudaStream_t stream, double *ops_per_s);
 }   // namespace sgb
 
@@ -60,8 +67,20 @@ struct Module {
     uint32_t mixed_variant = 1;    // precision 2: 0 FP64-residual refinement, 1 double-float state (default)
     uint64_t launches = 0;
     float last_ms = 0.0f;
+    // straggler hand-off: cells past `straggler_budget` step attempts in one launch are parked
+    // and finished by the cooperative kernel (one CTA per cell) on the same stream
+    uint32_t straggler_budget = 0;
+    SuspendRec *d_suspend = nullptr;
+    uint32_t *d_suspend_count = nullptr;
+    void *d_coop_image = nullptr;
+    CoopMech coop_head;
+    double *d_coop_scratch = nullptr;
+    uint32_t coop_grid = 0;
 };
 Module g;
+constexpr uint32_t kSuspendCap = 1u << 16;       // parked cells per launch
+constexpr uint32_t kResumeCtasPerSm = 8;         // cooperative CTAs per SM for parked cells
+constexpr uint32_t kResumeBlock = 64;            // threads per parked cell (KinMech mechanisms: n <= 32)
 
 const GpuKinTuning kDefaultTuning = {2u, 128u, 0u, 0u, 0.0f};   // CTA-synchronous queue, 128 threads, 255 registers
 
@@ -103,8 +122,37 @@ cudaError_t occupancy(uint32_t prec, const GpuKinTuning &t, int *blocks) {
     return occupancy_table_p2(t.kind, t.block, kTableBytes, blocks);
 }
 
-// Launches one advance of `A` with tuning `t` on the module stream.
-cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &A) {
+cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A);
+
+// Launches one advance of `A` with tuning `t` on the module stream; with a
+// straggler budget (precision 0 and the double-float mixed path), cells still
+// stepping after that many attempts are parked and finished by the
+// cooperative kernel right after (FP64: the same bits; mixed: its FP32-LU
+// cooperative path).
+cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &A0) {
+    if (A0.lanes == 0) return cudaSuccess;
+    const bool handoff = g.straggler_budget && g.d_coop_image && (prec == 0 || (prec == 2 && g.mixed_variant == 1));
+    if (!handoff) return launch_lanes(prec, t, A0);
+    DevArgs A = A0;
+    A.budget = g.straggler_budget;
+    A.suspend_cap = kSuspendCap;
+    A.suspend_count = g.d_suspend_count;
+    A.suspend = g.d_suspend;
+    cudaError_t e = cudaMemsetAsync(g.d_suspend_count, 0, sizeof(uint32_t), g.stream);
+    if (e == cudaSuccess) e = launch_lanes(prec, t, A);
+    if (e != cudaSuccess) return e;
+    DevArgs R = A;
+    R.budget = 0;
+    R.resume = 1;
+    R.tables = g.d_coop_image;
+    R.table_bytes = g.coop_head.bytes;
+    e = cudaMemsetAsync(g.d_cursor, 0, sizeof(uint32_t), g.stream);
+    if (e != cudaSuccess) return e;
+    return coop_resume_launch(prec == 0 ? 0 : 2, R, g.coop_head, g.d_coop_scratch, g.coop_grid, kResumeBlock, g.stream);
+}
+
+// The lane kernels (one cell per thread) for `A`.
+cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A) {
     if (A.lanes == 0) return cudaSuccess;
     Shape s;
     s.kind = t.kind;
@@ -233,6 +281,11 @@ SGB_API int32_t gpu_init(uint32_t device_index, uint64_t arena_bytes, GpuInfo *i
     if (e != cudaSuccess) return (int32_t)e;
     g.d_error = (uint32_t *)((uint8_t *)g.d_cursor + 128);
     cudaMemset(g.d_cursor, 0, 256);
+    if (!g.d_suspend) {
+        e = cudaMalloc((void **)&g.d_suspend, (size_t)kSuspendCap * sizeof(SuspendRec) + 256);
+        if (e != cudaSuccess) return (int32_t)e;
+        g.d_suspend_count = (uint32_t *)((uint8_t *)g.d_suspend + (size_t)kSuspendCap * sizeof(SuspendRec));
+    }
     if (!g.stream) {
         cudaEventCreate(&g.kin_start);
         cudaEventCreate(&g.kin_stop);
@@ -319,6 +372,25 @@ SGB_API int32_t gpu_kin_set_mech(const KinMech *mech, const KinMethod *method, c
     g.control = *control;
     g.generated = fnv1a(mech, sizeof(KinMech)) == air_ops_signature() && method_is_rodas3(method);
     g.have_mech = true;
+    // the cooperative image of the same mechanism, for the straggler hand-off
+    std::vector<uint8_t> coop;
+    if (coop_image(*mech, &coop)) {
+        memcpy(&g.coop_head, coop.data(), sizeof(CoopMech));
+        if (g.d_coop_image) cudaFree(g.d_coop_image);
+        if (g.d_coop_scratch) cudaFree(g.d_coop_scratch);
+        g.d_coop_image = nullptr;
+        g.d_coop_scratch = nullptr;
+        g.coop_grid = (uint32_t)g.sms * kResumeCtasPerSm;
+        const size_t a = coop_scratch_doubles_for(0, g.coop_head), b = coop_scratch_doubles_for(2, g.coop_head);
+        e = cudaMalloc(&g.d_coop_image, coop.size());
+        if (e == cudaSuccess) e = cudaMemcpy(g.d_coop_image, coop.data(), coop.size(), cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMalloc((void **)&g.d_coop_scratch, (a > b ? a : b) * 8 * g.coop_grid);
+        if (e != cudaSuccess) {
+            if (g.d_coop_image) cudaFree(g.d_coop_image);
+            g.d_coop_image = nullptr;
+            return (int32_t)e;
+        }
+    }
     return 0;
 }
 
@@ -442,7 +514,7 @@ SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuK
     struct Cand { uint32_t block, variant, ctas; };
     const Cand cands[] = {{32, 0, 0}, {64, 0, 0}, {128, 0, 0}, {64, 1, 0}, {128, 1, 0},
                           {128, 0, 1}, {64, 0, 2}, {64, 0, 3}, {128, 1, 2}, {128, 1, 3}};
-    const Cand sync_cands[] = {{256, 2, 1}, {128, 0, 2}, {128, 0, 1}, {128, 1, 3}, {128, 1, 4}, {512, 3, 1}};
+    const Cand sync_cands[] = {{128, 0, 2}, {256, 2, 1}, {128, 0, 1}, {128, 1, 4}, {512, 3, 1}};
     GpuKinTuning winner = g.tuning[launch->precision];
     winner.ms = 1e30f;
     const Cand *list = kind == 2 ? sync_cands : cands;
@@ -453,9 +525,13 @@ SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuK
         if (kind == 0 && c.ctas != 0) continue;
         {
             GpuKinTuning t = {kind, c.block, c.ctas, c.variant, 0.0f};
-            float ms = 0.0f;
-            e = advance_sync(launch, t, &ms);
-            copy_all(false);
+            float ms = 0.0f, best_ms = 1e30f;
+            for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {   // the faster of two runs
+                e = advance_sync(launch, t, &ms);
+                copy_all(false);
+                if (ms < best_ms) best_ms = ms;
+            }
+            ms = best_ms;
             if (e != cudaSuccess) break;
             if (ms < winner.ms) {
                 winner = t;
@@ -482,6 +558,18 @@ SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps) {
     if (sweeps < 1 || sweeps > 2) return (int32_t)cudaErrorInvalidValue;
     g.ir_sweeps = sweeps;
     return 0;
+}
+
+SGB_API int32_t gpu_kin_set_straggler_budget(uint32_t attempts) {
+    g.straggler_budget = attempts;
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_parked_cells(uint32_t *count) {
+    if (!g.ready || !count) return (int32_t)cudaErrorInvalidValue;
+    cudaError_t e = cudaMemcpyAsync(count, g.d_suspend_count, sizeof(uint32_t), cudaMemcpyDeviceToHost, g.stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(g.stream);
+    return (int32_t)e;
 }
 
 SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant) {

@@ -105,6 +105,20 @@ struct CoopCell {
         sync();
     }
 
+    // A parked cell: its scalar state from the record (load() read y, k, src and failed).
+    __device__ void restore(const SuspendRec &r) {
+        t = r.t;
+        h = r.h;
+        seg_end = r.seg_end;
+        applied = r.applied;
+        pending = (r.flags & 1u) != 0;
+        reject_last = (r.flags & 2u) != 0;
+        reject_more = (r.flags & 4u) != 0;
+        iterations = r.iterations;
+        transitions = r.transitions;
+        phase = kPhaseStepping;
+    }
+
     __device__ void store(const DevArgs &A, uint32_t cell) {
         const uint32_t p = A.padded;
         for (uint32_t s = tid; s < n; s += NT) A.y[(size_t)s * p + cell] = y[s];
@@ -499,13 +513,23 @@ __global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant_
         C.js = nullptr;
     }
     __syncthreads();
+    const uint32_t parked = A.resume ? min(*(volatile uint32_t *)A.suspend_count, A.suspend_cap) : 0u;
     for (;;) {
         if (threadIdx.x == 0) cell_s = atomicAdd(A.cursor, 1u);
         __syncthreads();
-        const uint32_t cell = cell_s;
+        const uint32_t idx = cell_s;
         __syncthreads();
-        if (cell >= A.lanes) break;
-        C.load(A, cell);
+        uint32_t cell = idx;
+        if (A.resume) {   // cells parked by a lane kernel of this launch
+            if (idx >= parked) break;
+            const SuspendRec r = A.suspend[idx];
+            cell = r.cell;
+            C.load(A, cell);
+            C.restore(r);
+        } else {
+            if (idx >= A.lanes) break;
+            C.load(A, cell);
+        }
         while (C.settle(A, cell)) C.attempt(A);
         C.store(A, cell);
     }
@@ -545,6 +569,25 @@ size_t coop_scratch_doubles(int prec, const CoopMech &h) {
 }
 
 }   // namespace
+
+size_t coop_smem_bytes_for(int prec, const CoopMech &h) { return coop_smem_bytes(prec, h); }
+size_t coop_scratch_doubles_for(int prec, const CoopMech &h) { return coop_scratch_doubles(prec, h); }
+
+// The cooperative kernel over the cells a lane kernel parked (A.resume set,
+// A.tables the coop image, A.cursor zeroed); `scratch` holds grid slots of
+// coop_scratch_doubles_for(prec) doubles.
+cudaError_t coop_resume_launch(int prec, const DevArgs &A, const CoopMech &head, double *scratch, uint32_t grid,
+                               uint32_t block, cudaStream_t s) {
+    void (*fn)(DevArgs, double *, uint64_t) = prec == 0 ? kin_coop_kernel<0> : kin_coop_kernel<2>;
+    const size_t smem = coop_smem_bytes(prec, head);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
+    fn<<<grid, block, smem, s>>>(A, scratch, coop_scratch_doubles(prec, head));
+    return cudaGetLastError();
+}
+
 }   // namespace sgb
 
 using namespace sgb;

@@ -135,6 +135,20 @@ struct DevArgs {
     uint32_t *error_flag;      // nonzero: a bounded wait ran out (tables not staged)
     const void *tables;        // table-driven ops: KinMech image in global memory
     uint32_t table_bytes;      // bytes to stage (multiple of 16)
+    // straggler hand-off (queue and static kernels, precisions 0 and 3): a cell that has
+    // taken `budget` step attempts in this launch parks its scalar state in `suspend` and
+    // leaves; a cooperative kernel finishes it (0 = never)
+    uint32_t budget;
+    uint32_t suspend_cap;
+    uint32_t *suspend_count;
+    struct SuspendRec *suspend;
+    uint32_t resume;           // cooperative kernel: take cells from the suspension list
+};
+
+// The scalar state of a parked cell (its y, h and counters are in the zone block).
+struct SuspendRec {
+    double t, h, seg_end, applied;
+    uint32_t cell, iterations, transitions, flags;   // flags: pending | reject_last << 1 | reject_more << 2
 };
 
 // Method coefficients known at compile time (Rodas3: kin_solver.h:382-391) or
@@ -191,7 +205,7 @@ struct Lane {
     float khi[kMixed ? R : 1], klo[kMixed ? R : 1], shi[kMixed ? N : 1], slo[kMixed ? N : 1];   // mixed: double-float k, src
     T t, h, seg_end, applied, duration, period, first, count;
     T steps, rejects, pulses, failed;
-    uint32_t iterations, transitions;
+    uint32_t iterations, transitions, attempts;
     int phase;
     bool pending, reject_last, reject_more;
     // per-attempt scratch
@@ -250,7 +264,26 @@ struct Lane {
         t = (T)0.0;
         applied = (T)0.0;
         transitions = 0;
+        attempts = 0;
         phase = kPhaseSegStart;
+    }
+
+    // Straggler hand-off: park the scalar state; false if the list is full (the lane keeps the cell).
+    __device__ __forceinline__ bool park(const DevArgs &A, uint32_t cell) {
+        const uint32_t slot = atomicAdd(A.suspend_count, 1u);
+        if (slot >= A.suspend_cap) return false;
+        SuspendRec r;
+        r.t = (double)t;
+        r.h = (double)h;
+        r.seg_end = (double)seg_end;
+        r.applied = (double)applied;
+        r.cell = cell;
+        r.iterations = iterations;
+        r.transitions = transitions;
+        r.flags = (pending ? 1u : 0u) | (reject_last ? 2u : 0u) | (reject_more ? 4u : 0u);
+        A.suspend[slot] = r;
+        phase = kPhaseDone;
+        return true;
     }
 
     // dbd_lanes.h:60-77: f32 lanes add their increment to the f64 storage.
@@ -321,6 +354,10 @@ struct Lane {
                 case kPhaseSegStart: seg_start(A); break;
                 case kPhaseSegFinish: seg_finish(A, cell); break;
                 case kPhaseStepping:
+                    if constexpr (PREC == 0) {
+                        if (A.budget && attempts >= A.budget && park(A, cell)) return false;
+                        ++attempts;
+                    }
                     if (++iterations > A.ctl.max_steps) {   // kin_solver.h:212-215
                         failed = (T)1.0;
                         phase = kPhaseSegFinish;
@@ -589,7 +626,7 @@ struct LaneDf {
     float khi[R], klo[R], shi[N], slo[N];
     double t, h, seg_end, applied, duration, period, first, count;
     double steps, rejects, pulses, failed;
-    uint32_t iterations, transitions;
+    uint32_t iterations, transitions, attempts;
     int phase;
     bool pending, reject_last, reject_more;
     float lu[NNZ];
@@ -627,7 +664,26 @@ struct LaneDf {
         t = 0.0;
         applied = 0.0;
         transitions = 0;
+        attempts = 0;
         phase = kPhaseSegStart;
+    }
+
+    // Straggler hand-off (see Lane::park); y goes to the zone block as hi + lo, exact in FP64.
+    __device__ __forceinline__ bool park(const DevArgs &A, uint32_t cell) {
+        const uint32_t slot = atomicAdd(A.suspend_count, 1u);
+        if (slot >= A.suspend_cap) return false;
+        SuspendRec r;
+        r.t = t;
+        r.h = h;
+        r.seg_end = seg_end;
+        r.applied = applied;
+        r.cell = cell;
+        r.iterations = iterations;
+        r.transitions = transitions;
+        r.flags = (pending ? 1u : 0u) | (reject_last ? 2u : 0u) | (reject_more ? 4u : 0u);
+        A.suspend[slot] = r;
+        phase = kPhaseDone;
+        return true;
     }
 
     __device__ __forceinline__ void store(const DevArgs &A, uint32_t i) {
@@ -684,6 +740,8 @@ struct LaneDf {
                 case kPhaseSegStart: seg_start(A); break;
                 case kPhaseSegFinish: seg_finish(A, cell); break;
                 case kPhaseStepping:
+                    if (A.budget && attempts >= A.budget && park(A, cell)) return false;
+                    ++attempts;
                     if (++iterations > A.ctl.max_steps) {
                         failed = 1.0;
                         phase = kPhaseSegFinish;

@@ -84,6 +84,7 @@ private:
 
 // Wide-index image for the cooperative kernels (coop.h); false if the model is not finalized.
 bool coop_image(const Model &m, std::vector<uint8_t> *out);
+bool coop_image(const KinMech &k, std::vector<uint8_t> *out);
 
 void define_air(Model *m);   // the shipped 17-species, 44-reaction humid-air mechanism
 uint64_t fnv1a(const void *data, uint64_t size);
