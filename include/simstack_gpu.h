@@ -383,6 +383,11 @@ SGB_API void kin_model_counts(const KinModelHandle *model, uint64_t *counts);
 /* Reference-layout tables; cudaErrorInvalidValue (1) if the mechanism exceeds them. */
 SGB_API int32_t kin_model_kinmech(const KinModelHandle *model, KinMech *out);
 SGB_API uint64_t kin_mech_signature(const KinMech *mech); /* FNV-1a over the record */
+/* The cooperative kernels' wide-index image (pattern bitmask, term lists, elimination lists) of a
+ * finalized model or of a KinMech; returns its size (0 if it cannot be built) and copies it to
+ * `out` when `capacity` suffices. The same mechanism gives the same bytes from either source. */
+SGB_API uint64_t kin_model_coop_image(const KinModelHandle *model, void *out, uint64_t capacity);
+SGB_API uint64_t kin_mech_coop_image(const KinMech *mech, void *out, uint64_t capacity);
 SGB_API void kin_model_rate_constants(const KinModelHandle *model, double T, double M, double *k);
 /* Rate constants for `cells` cells of a [reactions][padded] block from T and M per cell. */
 SGB_API void kin_model_rate_block(const KinModelHandle *model, const double *T, const double *M, uint32_t cells,

@@ -191,6 +191,8 @@ def lib() -> C.CDLL:
             "kin_model_counts": (None, [vp, C.POINTER(u64)]),
             "kin_model_kinmech": (i32, [vp, C.POINTER(KinMech)]),
             "kin_mech_signature": (u64, [C.POINTER(KinMech)]),
+            "kin_model_coop_image": (u64, [vp, vp, u64]),
+            "kin_mech_coop_image": (u64, [C.POINTER(KinMech), vp, u64]),
             "kin_model_rate_constants": (None, [vp, d, d, vp]),
             "kin_model_rate_block": (None, [vp, vp, vp, u32, u32, vp]),
             "kin_method_coefficients": (KinMethod, [u32]),

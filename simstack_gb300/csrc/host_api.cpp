@@ -76,6 +76,22 @@ SGB_API int32_t kin_model_kinmech(const KinModelHandle *h, KinMech *out) { retur
 
 SGB_API uint64_t kin_mech_signature(const KinMech *mech) { return fnv1a(mech, sizeof(KinMech)); }
 
+// The cooperative kernels' wide-index image of a finalized model or of a KinMech: its size
+// (0 if it cannot be built); copied to `out` when `capacity` suffices.
+SGB_API uint64_t kin_model_coop_image(const KinModelHandle *h, void *out, uint64_t capacity) {
+    std::vector<uint8_t> img;
+    if (!h || !coop_image(h->model, &img)) return 0;
+    if (out && capacity >= img.size()) memcpy(out, img.data(), img.size());
+    return img.size();
+}
+
+SGB_API uint64_t kin_mech_coop_image(const KinMech *mech, void *out, uint64_t capacity) {
+    std::vector<uint8_t> img;
+    if (!mech || !coop_image(*mech, &img)) return 0;
+    if (out && capacity >= img.size()) memcpy(out, img.data(), img.size());
+    return img.size();
+}
+
 SGB_API void kin_model_rate_constants(const KinModelHandle *h, double T, double M, double *k) { h->model.rate_constants(T, M, k); }
 
 SGB_API void kin_model_rate_block(const KinModelHandle *h, const double *T, const double *M, uint32_t cells, uint32_t padded,

@@ -1,6 +1,8 @@
 """Host-side mechanism compiler (the module's kin_model_*) against the oracle's
 restatement of the reference's builder, and the reference's numerical unit
 tests (test_kinetics.cpp:44-211) run on the oracle. CPU only."""
+import ctypes as C
+
 import numpy as np
 import pytest
 
@@ -155,3 +157,39 @@ def test_fixed_step_order(oracle_lib, method, order):
         y, t, h, st = m.integrate(method, ctl, [1.0], np.zeros(3), [A0, B0, 0.0], T, h0=T / steps)
         errs.append(abs(y[0] - exact))
     assert abs(np.log2(errs[2] / errs[3]) - order) < 0.3
+
+
+def coop_image(model=None, km=None) -> bytes:
+    L = sg.lib()
+    if model is not None:
+        size = L.kin_model_coop_image(model.h, None, 0)
+        buf = (C.c_uint8 * size)()
+        assert L.kin_model_coop_image(model.h, buf, size) == size
+    else:
+        size = L.kin_mech_coop_image(C.byref(km), None, 0)
+        buf = (C.c_uint8 * size)()
+        assert L.kin_mech_coop_image(C.byref(km), buf, size) == size
+    return bytes(buf)
+
+
+@pytest.mark.parametrize("which", ["air", "synthetic"])
+def test_coop_image_same_from_model_and_kinmech(which):
+    """The cooperative kernels' image is the same bytes whether it is built from
+    the model or from the reference-layout KinMech (the straggler hand-off builds
+    it from the KinMech that gpu_kin_set_mech receives)."""
+    pm = sg.Model.air() if which == "air" else sg.Model.synthetic(seed=5, species=24, reactions=80, bimolecular=0.7,
+                                                                  products=1)
+    a = coop_image(model=pm)
+    b = coop_image(km=pm.kinmech())
+    assert len(a) > 0 and a == b
+
+
+def test_coop_image_counts_large_mechanism(oracle_lib):
+    """Header counts of the 200-species image against the oracle's symbolic phase."""
+    pm, om = both_synthetic(oracle_lib, 3, 200, 1200, 1)
+    img = coop_image(model=pm)
+    n, R, ld, nj, fun_terms, jac_terms, l_entries, u_entries = np.frombuffer(img[:32], dtype=np.uint32)
+    lu_updates = np.frombuffer(img[32:40], dtype=np.uint64)[0]
+    oc = om.counts()
+    assert (n, R, ld) == (200, 1200, 201)
+    assert l_entries == oc["lower"] and u_entries == oc["upper"] and lu_updates == oc["updates"]
