@@ -218,8 +218,9 @@ SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant);
 /* Straggler hand-off (0 = off, the default): in one advance, a cell still stepping after
  * `attempts` step attempts on its lane is parked and finished right after by the cooperative
  * kernel (one CTA per cell, every thread sharing the cell's work), so a few very stiff cells
- * no longer run alone on single lanes at the end of the launch. Precision 0 keeps the same
- * bits; the double-float mixed path finishes parked cells on the cooperative mixed path. */
+ * no longer run alone on single lanes at the end of the launch. Parked cells finish in FP64
+ * (precision 0 keeps the same bits; the double-float mixed path's parked cells continue in
+ * FP64 from their mixed state). */
 SGB_API int32_t gpu_kin_set_straggler_budget(uint32_t attempts);
 /* Cells parked by the last advance that used the hand-off (waits for the module stream). */
 SGB_API int32_t gpu_kin_parked_cells(uint32_t *count);
@@ -314,7 +315,8 @@ typedef struct GpuServeRequest {
     uint32_t channel_cells;    /* cells per film channel, 1..4096 */
     uint32_t coupling_steps;
     uint32_t precision;        /* 0 FP64, 1 f32 Delta lanes, 2 mixed */
-    uint32_t mechanism;        /* 0 the shipped mechanism (generated kernels), 1 the engine's table mechanism */
+    uint32_t mechanism;        /* 0 the shipped mechanism (generated kernels), 1 the engine's table mechanism,
+                                  2 the engine's large mechanism (cooperative kernels; precision 0 or 2) */
     uint32_t reserved;
     double dt;                 /* coupling step, s */
     double velocity_m_s;       /* film flow speed */
@@ -342,6 +344,9 @@ typedef struct GpuServeStats {
 SGB_API int32_t gpu_serve_open(uint64_t hbm_budget_bytes, const KinControl *control);
 /* Table mechanism (mechanism = 1) and its method; only while the engine is empty. */
 SGB_API int32_t gpu_serve_set_mech(const KinMech *mech, const KinMethod *method);
+/* Large mechanism (mechanism = 2) from a finalized host model, up to 256 species; only while
+ * the engine is empty. */
+SGB_API int32_t gpu_serve_set_coop_mech(const KinModelHandle *model, const KinMethod *method);
 /* Queues a request; cudaErrorMemoryAllocation if it could never fit the budget. */
 SGB_API int32_t gpu_serve_submit(const GpuServeRequest *request, uint64_t *id);
 /* One scheduling round, non-blocking apart from uploads of newly admitted and

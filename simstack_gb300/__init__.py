@@ -173,6 +173,7 @@ def lib() -> C.CDLL:
             "gpu_serve_open": (i32, [u64, C.POINTER(KinControl)]),
             "gpu_serve_set_mech": (i32, [C.POINTER(KinMech), C.POINTER(KinMethod)]),
             "gpu_serve_submit": (i32, [C.POINTER(GpuServeRequest), C.POINTER(u64)]),
+            "gpu_serve_set_coop_mech": (i32, [vp, C.POINTER(KinMethod)]),
             "gpu_serve_progress": (i32, [C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
             "gpu_serve_cancel": (i32, [u64]),
             "gpu_serve_poll": (i32, [u64, C.POINTER(GpuServeStatus)]),
@@ -649,12 +650,19 @@ class Server:
         check(lib().gpu_serve_set_mech(C.byref(km), C.byref(meth)), "gpu_serve_set_mech")
         self._table_shape = (int(km.species_count), int(km.reaction_count))
 
+    def set_coop_mech(self, model: "Model", meth: KinMethod | None = None) -> None:
+        """Large mechanism for requests with mechanism = 2 (cooperative kernels)."""
+        meth = meth if meth is not None else method("rodas3")
+        self._coop = (model, meth)
+        check(lib().gpu_serve_set_coop_mech(model.h, C.byref(meth)), "gpu_serve_set_coop_mech")
+        self._coop_shape = (model.n, model.R)
+
     def submit(self, y0: np.ndarray, k: np.ndarray, coupling_steps: int, channel_cells: int, velocity_m_s: float,
                dx_m: float = 0.05, dt: float = 1.0, precision: int = 0, mechanism: int = 0) -> int:
         y0 = np.ascontiguousarray(y0, dtype=np.float64)
         k = np.ascontiguousarray(k, dtype=np.float64)
-        n, R = (17, 44) if mechanism == 0 else getattr(self, "_table_shape", (0, 0))
-        if mechanism in (0, 1) and (y0.shape[0] != n or k.shape != (R, y0.shape[1])):
+        n, R = (17, 44) if mechanism == 0 else getattr(self, "_table_shape" if mechanism == 1 else "_coop_shape", (0, 0))
+        if mechanism in (0, 1, 2) and (y0.shape[0] != n or k.shape != (R, y0.shape[1])):
             raise ValueError(f"request arrays {y0.shape} / {k.shape} do not match the mechanism ({n} species, {R} reactions)")
         q = GpuServeRequest(_p(y0), _p(k), y0.shape[1], channel_cells, coupling_steps, precision, mechanism, 0, dt,
                             velocity_m_s, dx_m)

@@ -37,7 +37,7 @@ cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
 uint64_t air_ops_signature();
 size_t coop_smem_bytes_for(int prec, const CoopMech &h);
 size_t coop_scratch_doubles_for(int prec, const CoopMech &h);
-cudaError_t coop_resume_launch(int prec, const DevArgs &A, const CoopMech &head, double *scratch, uint32_t grid,
+cudaError_t coop_launch(int prec, const DevArgs &A, const CoopMech &head, double *scratch, uint32_t grid,
                                uint32_t block, cudaStream_t s);
 cudaError_t run_probe(uint32_t kind, int sms, cudaStream_t stream, double *ops_per_s);
 }   // namespace sgb
@@ -126,9 +126,8 @@ cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A)
 
 // Launches one advance of `A` with tuning `t` on the module stream; with a
 // straggler budget (precision 0 and the double-float mixed path), cells still
-// stepping after that many attempts are parked and finished by the
-// cooperative kernel right after (FP64: the same bits; mixed: its FP32-LU
-// cooperative path).
+// stepping after that many attempts are parked and finished by the FP64
+// cooperative kernel right after (FP64 lanes: the same bits).
 cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &A0) {
     if (A0.lanes == 0) return cudaSuccess;
     const bool handoff = g.straggler_budget && g.d_coop_image && (prec == 0 || (prec == 2 && g.mixed_variant == 1));
@@ -148,7 +147,9 @@ cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &
     R.table_bytes = g.coop_head.bytes;
     e = cudaMemsetAsync(g.d_cursor, 0, sizeof(uint32_t), g.stream);
     if (e != cudaSuccess) return e;
-    return coop_resume_launch(prec == 0 ? 0 : 2, R, g.coop_head, g.d_coop_scratch, g.coop_grid, kResumeBlock, g.stream);
+    // parked cells finish on the FP64 cooperative path (for the mixed lanes too: on small
+    // mechanisms its step is shorter than the FP32 path's, which adds an FP64 refinement)
+    return coop_launch(0, R, g.coop_head, g.d_coop_scratch, g.coop_grid, kResumeBlock, g.stream);
 }
 
 // The lane kernels (one cell per thread) for `A`.

@@ -29,6 +29,7 @@ namespace sgb {
 namespace {
 
 constexpr uint32_t kCoopMaxSpecies = 256;   // register cache of a pivot row: 8 columns per lane
+constexpr size_t kCoopSmemLuF64Max = 64 * 1024;   // FP64 LUs up to this size live in shared memory (n <= ~90)
 constexpr uint32_t kCoopMaxCols = kCoopMaxSpecies / 32;
 
 struct CoopTab {
@@ -508,8 +509,9 @@ __global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant_
     if constexpr (PREC == 2) {
         C.a = (typename CoopCell<PREC>::Cf *)(lcnt_s + ((n + 7) / 8) * 8);   // 16-byte aligned
         C.js = g;
-    } else {
-        C.a = (typename CoopCell<PREC>::Cf *)g;
+    } else {   // FP64: small LUs in shared memory, large ones in per-CTA global scratch (L2)
+        const bool in_smem = (size_t)n * C.ld * sizeof(double) <= kCoopSmemLuF64Max;
+        C.a = in_smem ? (typename CoopCell<PREC>::Cf *)(lcnt_s + ((n + 7) / 8) * 8) : (typename CoopCell<PREC>::Cf *)g;
         C.js = nullptr;
     }
     __syncthreads();
@@ -556,10 +558,13 @@ struct CoopModule {
 CoopModule cm;
 constexpr uint32_t kCoopMaxCtasPerSm = 2;   // scratch slots per SM
 
-// Shared memory: doubles, x32 (256 floats), pattern (n x 8 words), lcnt (n u16, padded), mixed: a (n x ld floats).
+// Shared memory: doubles, x32 (256 floats), pattern (n x 8 words), lcnt (n u16, padded), then the LU:
+// mixed always (n x ld floats), FP64 when it fits kCoopSmemLuF64Max (n x ld doubles).
 size_t coop_smem_bytes(int prec, const CoopMech &h) {
     size_t b = (size_t)coop_smem_doubles(h.n, h.R) * 8 + kCoopMaxSpecies * 4 + (size_t)h.n * 32 + ((h.n + 7) / 8) * 16;
+    const size_t lu64 = (size_t)h.n * h.ld * sizeof(double);
     if (prec == 2) b += (size_t)h.n * h.ld * 4;
+    else if (lu64 <= kCoopSmemLuF64Max) b += lu64;
     return b;
 }
 
@@ -573,10 +578,10 @@ size_t coop_scratch_doubles(int prec, const CoopMech &h) {
 size_t coop_smem_bytes_for(int prec, const CoopMech &h) { return coop_smem_bytes(prec, h); }
 size_t coop_scratch_doubles_for(int prec, const CoopMech &h) { return coop_scratch_doubles(prec, h); }
 
-// The cooperative kernel over the cells a lane kernel parked (A.resume set,
-// A.tables the coop image, A.cursor zeroed); `scratch` holds grid slots of
-// coop_scratch_doubles_for(prec) doubles.
-cudaError_t coop_resume_launch(int prec, const DevArgs &A, const CoopMech &head, double *scratch, uint32_t grid,
+// The cooperative kernel on `A` (A.tables the coop image, A.cursor zeroed):
+// lanes [0, A.lanes), or with A.resume the cells a lane kernel parked;
+// `scratch` holds grid slots of coop_scratch_doubles_for(prec) doubles.
+cudaError_t coop_launch(int prec, const DevArgs &A, const CoopMech &head, double *scratch, uint32_t grid,
                                uint32_t block, cudaStream_t s) {
     void (*fn)(DevArgs, double *, uint64_t) = prec == 0 ? kin_coop_kernel<0> : kin_coop_kernel<2>;
     const size_t smem = coop_smem_bytes(prec, head);

@@ -39,6 +39,7 @@
 #include "kin_table.cuh"
 #include "mech.h"
 #include "mech_tables.h"
+#include "coop.h"
 
 namespace sgb {
 cudaError_t launch_air_p0(const Shape &, const DevArgs &, cudaStream_t);
@@ -58,6 +59,11 @@ cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
 cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
 uint64_t air_ops_signature();
+size_t coop_smem_bytes_for(int prec, const CoopMech &h);
+size_t coop_scratch_doubles_for(int prec, const CoopMech &h);
+cudaError_t coop_launch(int prec, const DevArgs &A, const CoopMech &head, double *scratch, uint32_t grid, uint32_t block,
+                        cudaStream_t s);
+const Model *model_of(const KinModelHandle *h);
 }   // namespace sgb
 
 using namespace sgb;
@@ -136,11 +142,14 @@ struct Request {
     GpuServeRequest desc;
     uint32_t n = 0, R = 0, padded = 0, rows = 0;
     bool generated = true;
+    bool coop = false;          // mechanism 2: the cooperative kernels
     std::vector<double> host;   // the zone block until admission, then the result rows
     uint64_t footprint = 0;     // device bytes while running
     double *d_block = nullptr;  // zone block [rows][padded]
     double *d_inlet = nullptr;  // [n] inlet state
     unsigned char *d_scratch = nullptr;   // queue cursor (+0), error flag (+128), table image (+256)
+    double *d_coop = nullptr;             // cooperative mechanism: per-CTA LU / Jacobian scratch
+    uint32_t coop_grid = 0;
     cudaStream_t stream = nullptr;
     cudaEvent_t step_done = nullptr;
     cudaGraphExec_t graph = nullptr;
@@ -165,6 +174,10 @@ struct Engine {
     KinMech table_mech;
     KinMethod table_method;
     bool have_table_mech = false;
+    void *d_coop_image = nullptr;   // mechanism 2
+    CoopMech coop_head;
+    KinMethod coop_method;
+    bool have_coop = false;
     KinControl control;
     int sms = 0;
 };
@@ -194,6 +207,7 @@ void release(Request *r) {
         if (r->d_block) cudaFreeAsync(r->d_block, r->stream);
         if (r->d_inlet) cudaFreeAsync(r->d_inlet, r->stream);
         if (r->d_scratch) cudaFreeAsync(r->d_scratch, r->stream);
+        if (r->d_coop) cudaFreeAsync(r->d_coop, r->stream);
         cudaStreamDestroy(r->stream);
     }
     if (r->step_done) cudaEventDestroy(r->step_done);
@@ -202,6 +216,7 @@ void release(Request *r) {
     r->step_done = nullptr;
     r->d_block = r->d_inlet = nullptr;
     r->d_scratch = nullptr;
+    r->d_coop = nullptr;
 }
 
 // Allocates and uploads an admitted request, then captures its coupling step.
@@ -212,6 +227,9 @@ cudaError_t admit(Request *r) {
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&r->d_block, r->host.size() * sizeof(double), r->stream);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&r->d_inlet, r->n * sizeof(double), r->stream);
     if (e == cudaSuccess) e = cudaMallocAsync((void **)&r->d_scratch, 256 + kTableBytes, r->stream);
+    if (e == cudaSuccess && r->coop)
+        e = cudaMallocAsync((void **)&r->d_coop,
+                            coop_scratch_doubles_for(q.precision, E.coop_head) * sizeof(double) * r->coop_grid, r->stream);
     if (e != cudaSuccess) return e;
     std::vector<double> inlet(r->n);
     for (uint32_t s = 0; s < r->n; ++s) inlet[s] = r->host[(size_t)s * r->padded];   // cell 0's initial state
@@ -219,7 +237,7 @@ cudaError_t admit(Request *r) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(r->d_inlet, inlet.data(), r->n * sizeof(double), cudaMemcpyHostToDevice, r->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(r->d_scratch, 0, 256, r->stream);   // cursor and error flag
     std::vector<unsigned char> image;
-    if (e == cudaSuccess && !r->generated) {
+    if (e == cudaSuccess && !r->generated && !r->coop) {
         image.resize(kTableBytes);
         table_image(&E.table_mech, image.data());
         e = cudaMemcpyAsync(r->d_scratch + 256, image.data(), kTableBytes, cudaMemcpyHostToDevice, r->stream);
@@ -249,7 +267,7 @@ cudaError_t admit(Request *r) {
     A.lanes = q.cells;
     A.duration = q.dt;
     A.ctl = E.control;
-    const KinMethod M = r->generated ? method_coefficients(2) : E.table_method;
+    const KinMethod M = r->generated ? method_coefficients(2) : r->coop ? E.coop_method : E.table_method;
     memcpy(A.ma, M.a, sizeof(A.ma));
     memcpy(A.mc, M.c, sizeof(A.mc));
     memcpy(A.mm, M.m, sizeof(A.mm));
@@ -263,6 +281,32 @@ cudaError_t admit(Request *r) {
     A.error_flag = (uint32_t *)(r->d_scratch + 128);
     A.tables = r->d_scratch + 256;
     A.table_bytes = kTableBytes;
+
+    if (r->coop) {   // the cooperative kernel: one CTA per cell
+        A.tables = E.d_coop_image;
+        A.table_bytes = E.coop_head.bytes;
+        const uint32_t block = q.precision == 0 ? 256u : 512u;
+        DevArgs idle = A;   // loads the kernel and sets its shared-memory size outside the capture
+        idle.lanes = 0;
+        e = coop_launch(q.precision, idle, E.coop_head, r->d_coop, 1, block, r->stream);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(r->stream);
+        if (e != cudaSuccess) return e;
+        cudaGraph_t graph = nullptr;
+        e = cudaStreamBeginCapture(r->stream, cudaStreamCaptureModeThreadLocal);
+        if (e != cudaSuccess) return e;
+        cudaError_t ce = cudaMemsetAsync(r->d_scratch, 0, sizeof(uint32_t), r->stream);
+        if (ce == cudaSuccess) ce = coop_launch(q.precision, A, E.coop_head, r->d_coop, r->coop_grid, block, r->stream);
+        if (ce == cudaSuccess)
+            ce = (cudaError_t)gpu_advect(A.y, P, r->n, q.cells, q.channel_cells, r->d_inlet, r->courant, r->substeps, r->stream);
+        e = cudaStreamEndCapture(r->stream, &graph);
+        if (ce != cudaSuccess || e != cudaSuccess) {
+            if (graph) cudaGraphDestroy(graph);
+            return ce != cudaSuccess ? ce : e;
+        }
+        e = cudaGraphInstantiate(&r->graph, graph, 0);
+        cudaGraphDestroy(graph);
+        return e;
+    }
 
     Shape sh;
     sh.kind = 2;   // CTA-synchronous persistent queue
@@ -358,6 +402,7 @@ SGB_API int32_t gpu_serve_open(uint64_t hbm_budget_bytes, const KinControl *cont
     E.finished = 0;
     E.graph_launches = 0;
     E.have_table_mech = false;
+    E.have_coop = false;
     E.control = control ? *control : KinControl{1e-4, 6.02214076e8, 1e-14, 0.0, 1e-9, 1000000u, 0, 1};
     E.open = true;
     return 0;
@@ -373,12 +418,39 @@ SGB_API int32_t gpu_serve_set_mech(const KinMech *mech, const KinMethod *method)
     return 0;
 }
 
+// Large mechanism (mechanism = 2, the cooperative kernels) from a finalized host model; only
+// while the engine is empty.
+SGB_API int32_t gpu_serve_set_coop_mech(const KinModelHandle *model, const KinMethod *method) {
+    if (!E.open || !model || !method || method->stages < 2 || method->stages > 4) return (int32_t)cudaErrorInvalidValue;
+    if (!E.running.empty() || !E.waiting.empty()) return (int32_t)cudaErrorNotReady;
+    const Model *m = model_of(model);
+    std::vector<uint8_t> img;
+    if (!m || !coop_image(*m, &img)) return (int32_t)cudaErrorInvalidValue;
+    CoopMech h;
+    memcpy(&h, img.data(), sizeof(h));
+    int max_smem = 0;
+    cudaError_t e = cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (coop_smem_bytes_for(2, h) > (size_t)max_smem) return (int32_t)cudaErrorInvalidValue;
+    if (E.d_coop_image) cudaFree(E.d_coop_image);
+    E.d_coop_image = nullptr;
+    E.have_coop = false;
+    e = cudaMalloc(&E.d_coop_image, img.size());
+    if (e == cudaSuccess) e = cudaMemcpy(E.d_coop_image, img.data(), img.size(), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return (int32_t)e;
+    E.coop_head = h;
+    E.coop_method = *method;
+    E.have_coop = true;
+    return 0;
+}
+
 SGB_API int32_t gpu_serve_submit(const GpuServeRequest *q, uint64_t *id) {
     if (!E.open || !q || !id || q->cells == 0 || !q->y0 || !q->k || q->coupling_steps == 0 || q->channel_cells == 0 ||
         q->channel_cells > kMaxChannelCells || !(q->dt > 0.0) || !(q->dt < 1e300) || !(q->velocity_m_s >= 0.0) ||
-        !(q->velocity_m_s < 1e300) || !(q->dx_m > 0.0) || q->precision > 2 || q->mechanism > 1)
+        !(q->velocity_m_s < 1e300) || !(q->dx_m > 0.0) || q->precision > 2 || q->mechanism > 2)
         return (int32_t)cudaErrorInvalidValue;
     if (q->mechanism == 1 && !E.have_table_mech) return (int32_t)cudaErrorInvalidValue;
+    if (q->mechanism == 2 && (!E.have_coop || q->precision == 1)) return (int32_t)cudaErrorInvalidValue;
     // Courant-0.9 substeps (nft.cpp:531-536)
     const double v = q->velocity_m_s;
     const double sub = v > 0.0 ? ceil(q->dt / (0.9 * q->dx_m / v)) : 1.0;
@@ -386,13 +458,19 @@ SGB_API int32_t gpu_serve_submit(const GpuServeRequest *q, uint64_t *id) {
     Request *r = new Request();
     r->desc = *q;
     r->generated = q->mechanism == 0;
-    r->n = r->generated ? 17u : E.table_mech.species_count;
-    r->R = r->generated ? 44u : E.table_mech.reaction_count;
+    r->coop = q->mechanism == 2;
+    r->n = r->generated ? 17u : r->coop ? E.coop_head.n : E.table_mech.species_count;
+    r->R = r->generated ? 44u : r->coop ? E.coop_head.R : E.table_mech.reaction_count;
+    if (r->coop) {
+        const uint32_t per_sm = q->precision == 0 ? 2u : 1u;
+        r->coop_grid = (uint32_t)E.sms * per_sm < q->cells ? (uint32_t)E.sms * per_sm : q->cells;
+    }
     r->padded = pad8(q->cells);
     r->rows = 3 * r->n + r->R + 8;
     r->substeps = (uint32_t)sub;
     r->courant = v * (q->dt / r->substeps) / q->dx_m;
     r->footprint = (uint64_t)r->rows * r->padded * sizeof(double) + r->n * sizeof(double) + 256 + kTableBytes;
+    if (r->coop) r->footprint += coop_scratch_doubles_for(q->precision, E.coop_head) * sizeof(double) * r->coop_grid;
     if (r->footprint > E.budget) {   // could never be admitted
         delete r;
         return (int32_t)cudaErrorMemoryAllocation;
@@ -550,5 +628,8 @@ SGB_API int32_t gpu_serve_close(void) {
     E.running.clear();
     E.in_use = 0;
     E.open = false;
+    if (E.d_coop_image) cudaFree(E.d_coop_image);
+    E.d_coop_image = nullptr;
+    E.have_coop = false;
     return (int32_t)cudaDeviceSynchronize();
 }

@@ -178,3 +178,46 @@ def test_invalid_requests():
             with pytest.raises(sg.GpuError):
                 srv.submit(z["y"][:, :64], z["k"][:, :64], **args)
         assert srv.stats()["waiting"] == 0
+
+
+@pytest.mark.parametrize("precision", [0, 2])
+def test_served_large_mechanism(oracle_lib, precision):
+    """mechanism = 2: a 60-species / 300-reaction synthetic mechanism through the
+    cooperative kernel inside the coupling graph; FP64 bit for bit against the
+    oracle's coupled computation, mixed within tolerance."""
+    pm = sg.Model.synthetic(seed=7, species=60, reactions=300, bimolecular=0.7, products=1)
+    om = oracle_lib.Mechanism()
+    for s in range(60):
+        om.add_species(f"S{s}", True)
+    for r in range(pm.R):
+        om.add_reaction(sg.model_equation(pm, r), "arr", (float(pm.k_const[r]), 0.0, 0.0))
+    om.finalize()
+    cells, cc, steps, v = 40, 16, 2, 0.05
+    z = sg.synthetic_cells(pm, cells, seed=8)
+    ctl = sg.control(rtol=1e-4, atol=1e-12, max_steps=200000)
+    with sg.Server(0, ctl) as srv:
+        srv.set_coop_mech(pm, sg.method("rodas3"))
+        rid = srv.submit(z["y"][:, :cells], z["k"][:, :cells], steps, cc, v, precision=precision, mechanism=2)
+        srv.drain(timeout_s=300)
+        st = srv.poll(rid)
+        assert st["state"] == "done", st
+        y, nsteps, failed = srv.result(rid)
+    ref = z.copy()
+    inlet = np.array(ref["y"][:, 0])
+    octl = oracle_lib.control(rtol=1e-4, atol=1e-12, max_steps=200000)
+    for _ in range(steps):
+        om.advance("rodas3", octl, ref.as_dict(), ref.padded, 0, cells, 1.0, 0, 1)
+        for b in range(0, cells, cc):
+            e = min(cells, b + cc)
+            row = np.ascontiguousarray(ref["y"][:, b:e])
+            oracle_lib.advect(row, inlet, st["courant"], st["substeps"])
+            ref["y"][:, b:e] = row
+    want = np.ascontiguousarray(ref["y"][:, :cells])
+    assert not failed.any()
+    if precision == 0:
+        assert y.tobytes() == want.tobytes()
+        assert nsteps.tobytes() == np.ascontiguousarray(ref["steps"][:cells]).tobytes()
+    else:
+        sig = want >= 1e-9 * want.sum(axis=0)
+        rel = np.abs(y - want)[sig] / want[sig]
+        assert rel.max() < 1e-6, rel.max()
