@@ -662,7 +662,7 @@ class Server:
         y0 = np.ascontiguousarray(y0, dtype=np.float64)
         k = np.ascontiguousarray(k, dtype=np.float64)
         n, R = (17, 44) if mechanism == 0 else getattr(self, "_table_shape" if mechanism == 1 else "_coop_shape", (0, 0))
-        if mechanism in (0, 1, 2) and (y0.shape[0] != n or k.shape != (R, y0.shape[1])):
+        if (n, R) != (0, 0) and (y0.shape[0] != n or k.shape != (R, y0.shape[1])):   # unset mechanisms: the engine refuses
             raise ValueError(f"request arrays {y0.shape} / {k.shape} do not match the mechanism ({n} species, {R} reactions)")
         q = GpuServeRequest(_p(y0), _p(k), y0.shape[1], channel_cells, coupling_steps, precision, mechanism, 0, dt,
                             velocity_m_s, dx_m)
