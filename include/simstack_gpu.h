@@ -222,6 +222,8 @@ SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant);
  * (precision 0 keeps the same bits; the double-float mixed path's parked cells continue in
  * FP64 from their mixed state). */
 SGB_API int32_t gpu_kin_set_straggler_budget(uint32_t attempts);
+/* Threads of the cooperative kernel per parked cell (32..256, multiple of 32; default 64). */
+SGB_API int32_t gpu_kin_set_straggler_block(uint32_t threads);
 /* Cells parked by the last advance that used the hand-off (waits for the module stream). */
 SGB_API int32_t gpu_kin_parked_cells(uint32_t *count);
 SGB_API uint32_t gpu_kin_get_mixed_variant(void);

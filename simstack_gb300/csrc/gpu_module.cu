@@ -70,6 +70,7 @@ struct Module {
     // straggler hand-off: cells past `straggler_budget` step attempts in one launch are parked
     // and finished by the cooperative kernel (one CTA per cell) on the same stream
     uint32_t straggler_budget = 0;
+    uint32_t straggler_block = 64;   // threads per parked cell
     SuspendRec *d_suspend = nullptr;
     uint32_t *d_suspend_count = nullptr;
     void *d_coop_image = nullptr;
@@ -80,7 +81,7 @@ struct Module {
 Module g;
 constexpr uint32_t kSuspendCap = 1u << 16;       // parked cells per launch
 constexpr uint32_t kResumeCtasPerSm = 8;         // cooperative CTAs per SM for parked cells
-constexpr uint32_t kResumeBlock = 64;            // threads per parked cell (KinMech mechanisms: n <= 32)
+
 
 const GpuKinTuning kDefaultTuning = {2u, 128u, 0u, 0u, 0.0f};   // CTA-synchronous queue, 128 threads, 255 registers
 
@@ -149,7 +150,7 @@ cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &
     if (e != cudaSuccess) return e;
     // parked cells finish on the FP64 cooperative path (for the mixed lanes too: on small
     // mechanisms its step is shorter than the FP32 path's, which adds an FP64 refinement)
-    return coop_launch(0, R, g.coop_head, g.d_coop_scratch, g.coop_grid, kResumeBlock, g.stream);
+    return coop_launch(0, R, g.coop_head, g.d_coop_scratch, g.coop_grid, g.straggler_block, g.stream);
 }
 
 // The lane kernels (one cell per thread) for `A`.
@@ -563,6 +564,12 @@ SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps) {
 
 SGB_API int32_t gpu_kin_set_straggler_budget(uint32_t attempts) {
     g.straggler_budget = attempts;
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_set_straggler_block(uint32_t threads) {
+    if (threads < 32 || threads > 256 || (threads & 31)) return (int32_t)cudaErrorInvalidValue;
+    g.straggler_block = threads;
     return 0;
 }
 

@@ -231,13 +231,20 @@ struct CoopCell {
     __device__ void factor(Cf ghinv) {
         for (uint32_t k = 0; k < n; ++k) {
             const uint32_t nl = lcnt[k];
-            const Cf inv = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
+            // 1/U(k,k) once (a division costs many FP64 instructions per warp), shared through red[4]
+            Cf *inv_s = (Cf *)(red + 4);
+            if (tid == 0) {
+                const Cf inv = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
+                a[(size_t)k * ld + k] = inv;
+                *inv_s = inv;
+            }
+            if (nl == 0) continue;   // nothing below the pivot: the next pivot reads none of this pivot's writes
+            sync();
+            const Cf inv = *inv_s;
             // L column k: l_i = a[i][k] / U(k,k)
             for (uint32_t i = k + 1 + tid; i < n; i += NT)
                 if (bit(i, k)) a[(size_t)i * ld + k] = a[(size_t)i * ld + k] * inv;
-            if (nl) sync();
-            if (tid == 0) a[(size_t)k * ld + k] = inv;
-            if (nl == 0) continue;   // nothing below the pivot: the next pivot reads none of this pivot's writes
+            sync();
             // pivot row k (final) cached per lane: columns k+1+lane+32c in the pattern
             const uint32_t width = n - 1 - k, chunks = (width + 31) / 32;
             Cf pv[kCoopMaxCols];
@@ -365,11 +372,15 @@ struct CoopCell {
         bool last = h_wanted >= remaining;
         double hs = last ? remaining : vmin(h_wanted, h_cap);
 
+        if (tid == 0) {   // the step's two divisions once, shared through red[2..3] (rhs synchronises)
+            red[2] = 1.0 / (hs * M::gamma0(A));
+            red[3] = 1.0 / hs;
+        }
         rhs(y);
         neg_jac(y);
-        const double ghinv = 1.0 / (hs * M::gamma0(A));
+        const double ghinv = red[2];
         factor((Cf)ghinv);
-        const double hinv = 1.0 / hs;
+        const double hinv = red[3];
 
         bool fcn_at_y = true;
         const int S = M::stages(A);
@@ -426,16 +437,17 @@ struct CoopCell {
             ytmp[s] = ynew;
         }
         sync();
-        if (tid == 0) {
+        if (tid == 0) {   // error norm and step factor once, shared through red[0..1]
             double e = 0.0;
             for (uint32_t s = 0; s < n; ++s) e = sgb_fma(qv[s], qv[s], e);
+            e = vsqrt(e * inv_n);
+            if (!is_finite_lane(e)) e = 1e10;
             red[0] = e;
+            red[1] = step_factor(e, M::order(A));
         }
         sync();
-        double err = vsqrt(red[0] * inv_n);
-        if (!is_finite_lane(err)) err = 1e10;
-
-        double fac = step_factor(err, M::order(A));
+        const double err = red[0];
+        double fac = red[1];
         bool ok = err <= 1.0 || hs <= h_min;
         if (A.ctl.fixed_step) {
             ok = true;
