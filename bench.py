@@ -493,9 +493,9 @@ def run_ours(args):
 # steps from ~150 to ~2,700 per cell over 60 s on these initial states (p50 ~280),
 # measured on the oracle (64-cell sample, seed 3).
 CONFIG3_P0 = 1e-2
-# Straggler hand-off budget: cells past this many step attempts in one advance (about 2x the p99 of
-# this workload's step counts) finish on the cooperative kernel.
-CONFIG3_BUDGET = 1200
+# Straggler hand-off budget (FP64): cells past this many step attempts in one advance (about the p99
+# of this workload's step counts) finish on the cooperative kernel; the module's default.
+CONFIG3_BUDGET = 600
 
 
 def run_config3(args):
@@ -515,7 +515,7 @@ def run_config3(args):
     zf = None
     for prec in (0, 2):
         launch.precision = prec
-        for kind, budget in ((0, 0), (2, 0), (2, CONFIG3_BUDGET)):
+        for kind, budget in ((0, 0), (2, 0), (2, CONFIG3_BUDGET)) if prec == 0 else ((0, 0), (2, 0)):
             mod.set_straggler_budget(budget)
             sg.check(L.gpu_copy_on_device(work, pristine, z.nbytes), "copy")
             t = mod.autotune(launch, kind=kind)
@@ -544,7 +544,7 @@ def run_config3(args):
                 with np.errstate(all="ignore"):
                     rel = (np.abs(a - b) / np.abs(b))[sig]
                 results[key]["rel_err_vs_fp64"] = {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99))}
-    mod.set_straggler_budget(0)
+    mod.set_straggler_budget(CONFIG3_BUDGET)
     steps = zf["steps"][:cells]   # FP64 path: the oracle's step counts
     best = min((k for k in results if k.startswith("mixed")), key=lambda k: results[k]["ms"])
     line = {"metric": "cell-integrations/s", "value": results[best]["value"], "unit": "cell-integrations/s",
@@ -559,8 +559,7 @@ def run_config3(args):
             "kernels": results,
             "queue_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue"]["ms"],
                                         "mixed": results["mixed_static"]["ms"] / results["mixed_queue"]["ms"]},
-            "handoff_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue_handoff"]["ms"],
-                                          "mixed": results["mixed_static"]["ms"] / results["mixed_queue_handoff"]["ms"]}}
+            "handoff_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue_handoff"]["ms"]}}
     print(json.dumps(line))
 
 

@@ -215,14 +215,14 @@ SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps);
  * LU and solves, stage right-hand sides accumulated in double-float, almost no FP64 work per species
  * (only the scalar step controller stays FP64). Default 1. */
 SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant);
-/* Straggler hand-off (0 = off, the default): in one advance, a cell still stepping after
- * `attempts` step attempts on its lane is parked and finished right after by the cooperative
- * kernel (one CTA per cell, every thread sharing the cell's work), so a few very stiff cells
- * no longer run alone on single lanes at the end of the launch. Parked cells finish in FP64
- * (precision 0 keeps the same bits; the double-float mixed path's parked cells continue in
- * FP64 from their mixed state). */
+/* Straggler hand-off for precision 0 (0 = off; default 600): in one advance, a cell still
+ * stepping after `attempts` step attempts on its lane is parked and finished right after by the
+ * FP64 cooperative kernel (one CTA per cell, every thread sharing the cell's work), so a few very
+ * stiff cells no longer run alone on single lanes at the end of the launch; the results keep
+ * the same bits. The mixed path does not hand off: its lanes' FP32-pipe steps are shorter
+ * than the cooperative FP64 steps. */
 SGB_API int32_t gpu_kin_set_straggler_budget(uint32_t attempts);
-/* Threads of the cooperative kernel per parked cell (32..256, multiple of 32; default 64). */
+/* Threads of the cooperative kernel per parked cell (32..256, multiple of 32; default 128). */
 SGB_API int32_t gpu_kin_set_straggler_block(uint32_t threads);
 /* Cells parked by the last advance that used the hand-off (waits for the module stream). */
 SGB_API int32_t gpu_kin_parked_cells(uint32_t *count);

@@ -632,6 +632,7 @@ def dbd_commit_pulses(z: ZoneBlock) -> None:
 
 
 SERVE_STATES = ("waiting", "running", "done", "failed", "cancelled")
+DEFAULT_STRAGGLER_BUDGET = 600   # the module's default FP64 hand-off budget (gpu_kin_set_straggler_budget)
 
 
 class Server:

@@ -69,8 +69,8 @@ struct Module {
     float last_ms = 0.0f;
     // straggler hand-off: cells past `straggler_budget` step attempts in one launch are parked
     // and finished by the cooperative kernel (one CTA per cell) on the same stream
-    uint32_t straggler_budget = 0;
-    uint32_t straggler_block = 64;   // threads per parked cell
+    uint32_t straggler_budget = 600;  // FP64 step attempts per launch before a cell is handed on
+    uint32_t straggler_block = 128;   // threads per parked cell
     SuspendRec *d_suspend = nullptr;
     uint32_t *d_suspend_count = nullptr;
     void *d_coop_image = nullptr;
@@ -126,12 +126,13 @@ cudaError_t occupancy(uint32_t prec, const GpuKinTuning &t, int *blocks) {
 cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A);
 
 // Launches one advance of `A` with tuning `t` on the module stream; with a
-// straggler budget (precision 0 and the double-float mixed path), cells still
-// stepping after that many attempts are parked and finished by the FP64
-// cooperative kernel right after (FP64 lanes: the same bits).
+// straggler budget (precision 0), cells still stepping after that many
+// attempts are parked and finished by the FP64 cooperative kernel right after,
+// with the same bits. (The mixed lanes' FP32-pipe steps are shorter than the
+// cooperative FP64 steps, so they keep their cells.)
 cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &A0) {
     if (A0.lanes == 0) return cudaSuccess;
-    const bool handoff = g.straggler_budget && g.d_coop_image && (prec == 0 || (prec == 2 && g.mixed_variant == 1));
+    const bool handoff = g.straggler_budget && g.d_coop_image && prec == 0;
     if (!handoff) return launch_lanes(prec, t, A0);
     DevArgs A = A0;
     A.budget = g.straggler_budget;
@@ -148,8 +149,6 @@ cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &
     R.table_bytes = g.coop_head.bytes;
     e = cudaMemsetAsync(g.d_cursor, 0, sizeof(uint32_t), g.stream);
     if (e != cudaSuccess) return e;
-    // parked cells finish on the FP64 cooperative path (for the mixed lanes too: on small
-    // mechanisms its step is shorter than the FP32 path's, which adds an FP64 refinement)
     return coop_launch(0, R, g.coop_head, g.d_coop_scratch, g.coop_grid, g.straggler_block, g.stream);
 }
 

@@ -1,7 +1,6 @@
-"""Straggler hand-off: cells still stepping after a budget of step attempts are
-parked by the lane kernels and finished by the cooperative kernel. FP64 keeps
-every bit of the oracle (the reference's algorithm); the mixed path stays
-within its accuracy bounds."""
+"""Straggler hand-off: FP64 cells still stepping after a budget of step attempts
+are parked by the lane kernels and finished by the cooperative kernel, keeping
+every bit of the oracle (the reference's algorithm)."""
 import numpy as np
 import pytest
 
@@ -14,7 +13,7 @@ pytestmark = pytest.mark.gpu
 def budget(module, request):
     module.set_straggler_budget(request.param)
     yield request.param
-    module.set_straggler_budget(0)
+    module.set_straggler_budget(sg.DEFAULT_STRAGGLER_BUDGET)
 
 
 def source_cells(cells, seed=3):
@@ -64,16 +63,15 @@ def test_f64_handoff_pulsed_zones(module, oracle_lib, budget):
 
 
 @pytest.mark.parametrize("budget", [40], indirect=True)
-def test_mixed_handoff_accuracy(module, oracle_lib, budget):
+def test_mixed_keeps_its_cells(module, oracle_lib, budget):
+    """The mixed path does not hand off (its FP32-pipe lane steps are shorter than the
+    cooperative FP64 steps): the same bits with and without a budget."""
     module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
-    z = source_cells(1024, seed=4)
-    ref = z.copy()
-    module.integrate(z, 5.0, precision=2)
-    assert module.parked_cells() > 0
-    oracle_lib.Mechanism.air().advance("rodas3", oracle_lib.control(), ref.as_dict(), ref.padded, 0, ref.padded, 5.0, 0, 0)
-    b, a = ref["y"], z["y"]
-    sig = b >= 1e-12 * b.sum(axis=0)
-    with np.errstate(all="ignore"):
-        rel = (np.abs(a - b) / np.abs(b))[sig]
-    assert z["failed"].max() == 0.0
-    assert np.quantile(rel, 0.99) < 1e-5 and rel.max() < 1e-2, (rel.max(), np.quantile(rel, 0.99))
+    z = source_cells(512, seed=4)
+    a = z.copy()
+    module.integrate(a, 2.0, precision=2)
+    module.set_straggler_budget(0)
+    b = z.copy()
+    module.integrate(b, 2.0, precision=2)
+    for name in ("y", "h", "steps", "rejects", "failed"):
+        assert a[name].tobytes() == b[name].tobytes(), name
