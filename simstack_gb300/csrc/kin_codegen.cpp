@@ -101,7 +101,9 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
     fprintf(f, "    }\n\n");
 
     // -J into the compact LU storage
-    fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void neg_jac(const T *__restrict__ k, const T *__restrict__ y, T *__restrict__ a) {\n");
+    // LU storage element e of a lane lives at a[e * S]: S = 1 for a per-lane array, or the CTA's
+    // thread count for shared-memory storage interleaved across the CTA's lanes
+    fprintf(f, "    template <class T, int S = 1>\n    static __device__ __forceinline__ void neg_jac(const T *__restrict__ k, const T *__restrict__ y, T *__restrict__ a) {\n");
     std::vector<uint8_t> written(S.nnz, 0);
     std::vector<std::string> body;
     for (uint32_t r = 0; r < R; ++r) {
@@ -115,43 +117,43 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
                 int c = -rx.net[e].second;
                 uint32_t idx = rx.jac_slot[p][e];
                 if (!written[idx] && (c == 1 || c == -1))
-                    fprintf(f, "          a[%u] = %s(d);\n", idx, c == 1 ? "sgb_first_pos" : "sgb_first_neg");
+                    fprintf(f, "          a[%u * S] = %s(d);\n", idx, c == 1 ? "sgb_first_pos" : "sgb_first_neg");
                 else if (!written[idx])
-                    fprintf(f, "          a[%u] = sgb_fma((T)%d.0, d, (T)0.0);\n", idx, c);
+                    fprintf(f, "          a[%u * S] = sgb_fma((T)%d.0, d, (T)0.0);\n", idx, c);
                 else
-                    fprintf(f, "          a[%u] = sgb_fma((T)%d.0, d, a[%u]);\n", idx, c, idx);
+                    fprintf(f, "          a[%u * S] = sgb_fma((T)%d.0, d, a[%u * S]);\n", idx, c, idx);
                 written[idx] = 1;
             }
             fprintf(f, "        }\n");
         }
     }
     for (uint32_t i = 0; i < S.nnz; ++i)
-        if (!written[i]) fprintf(f, "        a[%u] = (T)0.0;\n", i);
+        if (!written[i]) fprintf(f, "        a[%u * S] = (T)0.0;\n", i);
     fprintf(f, "    }\n\n");
 
     // in-place no-pivot LU of I*ghinv - J; the diagonal keeps 1/U(i,i)
-    fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void factor(T ghinv, T *__restrict__ a) {\n");
+    fprintf(f, "    template <class T, int S = 1>\n    static __device__ __forceinline__ void factor(T ghinv, T *__restrict__ a) {\n");
     for (uint32_t i = 0; i < n; ++i) {
         for (uint32_t d = S.div_begin[i]; d < S.div_begin[i + 1]; ++d) {
             const Symbolic::Div &dv = S.divs[d];
-            fprintf(f, "        { const T l = a[%u] * a[%u]; a[%u] = l;\n", dv.ik, dv.kk, dv.ik);
+            fprintf(f, "        { const T l = a[%u * S] * a[%u * S]; a[%u * S] = l;\n", dv.ik, dv.kk, dv.ik);
             for (uint32_t s = dv.sub_begin; s < dv.sub_end; ++s)
-                fprintf(f, "          a[%u] = sgb_fma(-l, a[%u], a[%u]);\n", S.subs[s].ij, S.subs[s].kj, S.subs[s].ij);
+                fprintf(f, "          a[%u * S] = sgb_fma(-l, a[%u * S], a[%u * S]);\n", S.subs[s].ij, S.subs[s].kj, S.subs[s].ij);
             fprintf(f, "        }\n");
         }
-        fprintf(f, "        a[%u] = (T)1.0 / (a[%u] + ghinv);\n", S.diag[i], S.diag[i]);
+        fprintf(f, "        a[%u * S] = (T)1.0 / (a[%u * S] + ghinv);\n", S.diag[i], S.diag[i]);
     }
     fprintf(f, "    }\n\n");
 
     // forward (unit L, ascending column) and backward (U, descending column)
-    fprintf(f, "    template <class T>\n    static __device__ __forceinline__ void solve(const T *__restrict__ a, T *__restrict__ x) {\n");
+    fprintf(f, "    template <class T, int S = 1>\n    static __device__ __forceinline__ void solve(const T *__restrict__ a, T *__restrict__ x) {\n");
     for (uint32_t i = 0; i < n; ++i)
         for (uint32_t e = S.lower_begin[i]; e < S.lower_begin[i + 1]; ++e)
-            fprintf(f, "        x[%u] = sgb_fma(-a[%u], x[%u], x[%u]);\n", i, S.lower[e].index, S.lower[e].col, i);
+            fprintf(f, "        x[%u] = sgb_fma(-a[%u * S], x[%u], x[%u]);\n", i, S.lower[e].index, S.lower[e].col, i);
     for (uint32_t ii = n; ii-- > 0;) {
         for (uint32_t e = S.upper_begin[ii]; e < S.upper_begin[ii + 1]; ++e)
-            fprintf(f, "        x[%u] = sgb_fma(-a[%u], x[%u], x[%u]);\n", ii, S.upper[e].index, S.upper[e].col, ii);
-        fprintf(f, "        x[%u] = x[%u] * a[%u];\n", ii, ii, S.diag[ii]);
+            fprintf(f, "        x[%u] = sgb_fma(-a[%u * S], x[%u], x[%u]);\n", ii, S.upper[e].index, S.upper[e].col, ii);
+        fprintf(f, "        x[%u] = x[%u] * a[%u * S];\n", ii, ii, S.diag[ii]);
     }
     fprintf(f, "    }\n\n");
 

@@ -222,6 +222,8 @@ struct Lane {
     double rr[kMixed ? N : 1];                 // mixed: residual
     float x32[kMixed ? N : 1];
 
+    static constexpr size_t kSmemBytes = 0;
+    __device__ __forceinline__ void bind(unsigned char *) {}
     __device__ __forceinline__ uint32_t n() const { return ops.n(); }
 
     // dbd_lanes.h:28-58: storage is f64; f32 lanes round on load.
@@ -617,9 +619,13 @@ __device__ __forceinline__ Df df_prod_f(float a, float b) {   // exact product o
     return Df{p, fmaf(a, b, -p)};
 }
 
-template <class Ops, class M>
+// kLuStride > 0: the LU lives in shared memory, interleaved across the CTA's
+// lanes (element e of lane t at [e * kLuStride + t]: consecutive lanes hit
+// consecutive banks), instead of in the lane's registers / local memory.
+template <class Ops, class M, int kLuStride = 0>
 struct LaneDf {
     static constexpr int N = Ops::N, R = Ops::R, NNZ = Ops::NNZ, S = M::kStages;
+    static constexpr size_t kSmemBytes = kLuStride ? (size_t)NNZ * kLuStride * sizeof(float) : 0;
 
     Ops ops;
     float yhi[N], ylo[N];
@@ -629,12 +635,16 @@ struct LaneDf {
     uint32_t iterations, transitions, attempts;
     int phase;
     bool pending, reject_last, reject_more;
-    float lu[NNZ];
+    float lu_r[kLuStride ? 1 : NNZ];
+    float *lu_s;
     float fhi[N], flo[N];
     float K[S][N];
     float d32[N], df32[N];
     float nhi[N], nlo[N];
 
+    __device__ __forceinline__ void bind(unsigned char *smem) {
+        if constexpr (kLuStride > 0) lu_s = (float *)smem + threadIdx.x;
+    }
     __device__ __forceinline__ uint32_t n() const { return ops.n(); }
 
     __device__ __forceinline__ void load(const DevArgs &A, uint32_t i) {
@@ -768,9 +778,16 @@ struct LaneDf {
         const float hs32 = (float)hs;
 
         ops.fun_df(khi, klo, shi, slo, yhi, ylo, fhi, flo);
-        ops.neg_jac(khi, yhi, lu);
-        if constexpr (kSync) __syncthreads();
-        ops.factor(1.0f / (hs32 * (float)M::gamma0(A)), lu);
+        const float g32 = 1.0f / (hs32 * (float)M::gamma0(A));
+        if constexpr (kLuStride > 0) {
+            ops.template neg_jac<kLuStride>(khi, yhi, lu_s);
+            if constexpr (kSync) __syncthreads();
+            ops.template factor<kLuStride>(g32, lu_s);
+        } else {
+            ops.neg_jac(khi, yhi, lu_r);
+            if constexpr (kSync) __syncthreads();
+            ops.factor(g32, lu_r);
+        }
         if constexpr (kSync) __syncthreads();
         const float hinv = 1.0f / hs32;
 
@@ -811,7 +828,8 @@ struct LaneDf {
                 }
                 K[st][s] = b.hi + b.lo;
             }
-            ops.solve(lu, K[st]);
+            if constexpr (kLuStride > 0) ops.template solve<kLuStride>(lu_s, K[st]);
+            else ops.solve(lu_r, K[st]);
             if constexpr (kSync) __syncthreads();
         }
 
@@ -874,10 +892,7 @@ struct LaneDf {
     }
 };
 
-// The lane type of a precision: 0 FP64, 1 f32 Delta, 2 mixed with FP64
-// refinement, 3 mixed with double-float state.
-template <class Ops, class M, int PREC> struct LaneOf { typedef Lane<Ops, M, PREC> type; };
-template <class Ops, class M> struct LaneOf<Ops, M, 3> { typedef LaneDf<Ops, M> type; };
+
 
 // ---------------------------------------------------------------------------
 // Generated straight-line ops (kin_codegen.cpp) as an Ops object.
@@ -895,13 +910,16 @@ template <class Ops, class M> struct LaneOf<Ops, M, 3> { typedef LaneDf<Ops, M> 
 template <class G>
 struct GenOps {
     static constexpr int N = G::N, R = G::R, NNZ = G::NNZ, NJ = G::NJ;
+    static constexpr bool kStridedLu = true;   // the LU ops take a storage stride (shared-memory LU)
     __device__ __forceinline__ uint32_t n() const { return (uint32_t)N; }
     __device__ __forceinline__ uint32_t r() const { return (uint32_t)R; }
     __device__ __forceinline__ bool init(const DevArgs &, unsigned char *) { return true; }
     template <class T> __device__ SGB_OPS_QUALIFIER void fun(const T *k, const T *src, const T *y, T *f) const { G::fun(k, src, y, f); }
-    template <class T> __device__ SGB_OPS_QUALIFIER void neg_jac(const T *k, const T *y, T *a) const { G::neg_jac(k, y, a); }
-    template <class T> __device__ SGB_OPS_QUALIFIER void factor(T ghinv, T *a) const { G::factor(ghinv, a); }
-    template <class T> __device__ SGB_OPS_QUALIFIER void solve(const T *a, T *x) const { G::solve(a, x); }
+    template <int S = 1, class T> __device__ SGB_OPS_QUALIFIER void neg_jac(const T *k, const T *y, T *a) const {
+        G::template neg_jac<T, S>(k, y, a);
+    }
+    template <int S = 1, class T> __device__ SGB_OPS_QUALIFIER void factor(T ghinv, T *a) const { G::template factor<T, S>(ghinv, a); }
+    template <int S = 1, class T> __device__ SGB_OPS_QUALIFIER void solve(const T *a, T *x) const { G::template solve<T, S>(a, x); }
     __device__ SGB_OPS_QUALIFIER void fun_df(const float *khi, const float *klo, const float *shi, const float *slo, const float *yhi,
                                              const float *ylo, float *fhi, float *flo) const {
         G::fun_df(khi, klo, shi, slo, yhi, ylo, fhi, flo);

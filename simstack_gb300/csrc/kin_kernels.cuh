@@ -25,6 +25,20 @@ template <> struct Budget<1> { static constexpr int kThreads = 128, kMinBlocks =
 template <> struct Budget<2> { static constexpr int kThreads = 256, kMinBlocks = 1; };
 template <> struct Budget<3> { static constexpr int kThreads = 512, kMinBlocks = 1; };   // 128 registers
 
+// Build-time switch: the double-float mixed lanes keep their LU in shared memory
+// (generated ops, CTAs of up to 256 threads) instead of registers / local memory.
+#ifndef SGB_SHARED_LU
+#define SGB_SHARED_LU 0
+#endif
+
+// The lane type of a precision: 0 FP64, 1 f32 Delta, 2 mixed with FP64
+// refinement, 3 mixed with double-float state.
+template <class Ops, class M, int PREC, int V> struct LaneOf { typedef Lane<Ops, M, PREC> type; };
+template <class Ops, class M, int V> struct LaneOf<Ops, M, 3, V> {
+    static constexpr int kStride = (SGB_SHARED_LU && Ops::kStridedLu && Budget<V>::kThreads <= 256) ? Budget<V>::kThreads : 0;
+    typedef LaneDf<Ops, M, kStride> type;
+};
+
 // Both kernels keep every lane of a warp in the loop until the whole warp is
 // out of work, and vote (__any_sync) once per iteration: the vote is a
 // reconvergence point, so all lanes that need a step attempt run it together
@@ -34,11 +48,12 @@ template <> struct Budget<3> { static constexpr int kThreads = 512, kMinBlocks =
 template <class Ops, class M, int PREC, int V>
 __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_static_kernel(const __grid_constant__ DevArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
-    typename LaneOf<Ops, M, PREC>::type L;
+    typename LaneOf<Ops, M, PREC, V>::type L;
     if (!L.ops.init(A, smem)) {
         if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
         return;
     }
+    L.bind(smem);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool have = i < A.lanes;
     if (have) L.load(A, i);
@@ -59,11 +74,12 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
 template <class Ops, class M, int PREC, int V>
 __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_queue_kernel(const __grid_constant__ DevArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
-    typename LaneOf<Ops, M, PREC>::type L;
+    typename LaneOf<Ops, M, PREC, V>::type L;
     if (!L.ops.init(A, smem)) {
         if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
         return;
     }
+    L.bind(smem);
     bool have = false, exhausted = false;
     uint32_t cell = 0;
     for (;;) {
@@ -100,11 +116,12 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
 template <class Ops, class M, int PREC, int V>
 __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) kin_queue_cta_kernel(const __grid_constant__ DevArgs A) {
     extern __shared__ __align__(128) unsigned char smem[];
-    typename LaneOf<Ops, M, PREC>::type L;
+    typename LaneOf<Ops, M, PREC, V>::type L;
     if (!L.ops.init(A, smem)) {
         if (threadIdx.x == 0) atomicExch(A.error_flag, 1u);
         return;
     }
+    L.bind(smem);
     if (A.lanes == 0) return;
     L.load(A, 0);   // a finite state for lanes that never get a cell
     bool have = false, exhausted = false;
@@ -156,24 +173,40 @@ void (*kernel_for(uint32_t kind, uint32_t variant))(DevArgs) {
     return kind == 0 ? kin_static_kernel<Ops, M, PREC, 0> : kin_queue_kernel<Ops, M, PREC, 0>;
 }
 
+// Shared memory the lane itself needs (a shared-memory LU), per kernel variant.
+template <class Ops, class M, int PREC, int kVariants>
+size_t lane_smem_for(uint32_t kind, uint32_t variant) {
+    constexpr int V1 = kVariants > 1 ? 1 : 0, V2 = kVariants > 1 ? 2 : 0, V3 = kVariants > 1 ? 3 : 0;
+    if (kVariants > 1 && variant == 1) return LaneOf<Ops, M, PREC, V1>::type::kSmemBytes;
+    if (kind == 2 && kVariants > 1 && variant == 2) return LaneOf<Ops, M, PREC, V2>::type::kSmemBytes;
+    if (kind == 2 && kVariants > 1 && variant == 3) return LaneOf<Ops, M, PREC, V3>::type::kSmemBytes;
+    return LaneOf<Ops, M, PREC, 0>::type::kSmemBytes;
+}
+
 template <class Ops, class M, int PREC, int kVariants = 2>
 cudaError_t launch_one(const Shape &s, const DevArgs &A, cudaStream_t stream) {
     void (*fn)(DevArgs) = kernel_for<Ops, M, PREC, kVariants>(s.kind, s.variant);
-    if (s.smem == 0) {   // no shared memory: give the unified L1/shared array to L1 (local-memory spills live there)
+    const size_t smem = s.smem + lane_smem_for<Ops, M, PREC, kVariants>(s.kind, s.variant);
+    if (smem == 0) {   // no shared memory: give the unified L1/shared array to L1 (local-memory spills live there)
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 0);
         if (e != cudaSuccess) return e;
     }
-    if (s.smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.smem);
+    if (smem > 48 * 1024) {
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
     }
-    fn<<<s.grid, s.block, s.smem, stream>>>(A);
+    fn<<<s.grid, s.block, smem, stream>>>(A);
     return cudaGetLastError();
 }
 
 template <class Ops, class M, int PREC, int kVariants = 2>
 cudaError_t occupancy_one(uint32_t kind, uint32_t variant, uint32_t block, size_t smem, int *blocks_per_sm) {
     void (*fn)(DevArgs) = kernel_for<Ops, M, PREC, kVariants>(kind, variant);
+    smem += lane_smem_for<Ops, M, PREC, kVariants>(kind, variant);
+    if (smem > 48 * 1024) {   // the occupancy query honours the attribute, so set it first
+        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+    }
     return cudaOccupancyMaxActiveBlocksPerMultiprocessor(blocks_per_sm, fn, (int)block, smem);
 }
 

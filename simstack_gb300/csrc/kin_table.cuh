@@ -18,6 +18,7 @@ constexpr uint32_t kTableBytes = kJacMaskOffset + KIN_MAX_NNZ / 8;
 
 struct TableOps {
     static constexpr int N = KIN_MAX_SPECIES, R = KIN_MAX_REACTIONS, NNZ = KIN_MAX_NNZ, NJ = KIN_MAX_NNZ;
+    static constexpr bool kStridedLu = false;   // shared memory holds the staged tables
     const KinMech *m;
 
     __device__ __forceinline__ uint32_t n() const { return m->species_count; }
