@@ -222,6 +222,9 @@ SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant);
  * the same bits. The mixed path does not hand off: its lanes' FP32-pipe steps are shorter
  * than the cooperative FP64 steps. */
 SGB_API int32_t gpu_kin_set_straggler_budget(uint32_t attempts);
+/* Per-thread stack (local memory) reservation of the current context: set it when set_bytes
+ * is nonzero; *current receives the value in force. */
+SGB_API int32_t gpu_stack_limit(uint64_t set_bytes, uint64_t *current);
 /* Threads of the cooperative kernel per parked cell (32..256, multiple of 32; default 128). */
 SGB_API int32_t gpu_kin_set_straggler_block(uint32_t threads);
 /* Cells parked by the last advance that used the hand-off (waits for the module stream). */

@@ -159,6 +159,7 @@ def lib() -> C.CDLL:
             "gpu_kin_get_mixed_variant": (u32, []),
             "gpu_kin_set_straggler_budget": (i32, [u32]),
             "gpu_kin_set_straggler_block": (i32, [u32]),
+            "gpu_stack_limit": (i32, [u64, C.POINTER(u64)]),
             "gpu_kin_parked_cells": (i32, [C.POINTER(u32)]),
             "gpu_probe_throughput": (i32, [u32, C.POINTER(d)]),
             "gpu_stream": (vp, []),

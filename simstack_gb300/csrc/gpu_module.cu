@@ -561,6 +561,17 @@ SGB_API int32_t gpu_kin_set_refinement(uint32_t sweeps) {
     return 0;
 }
 
+// Per-thread stack (local memory) reservation of the context: it grows to the largest
+// frame any launched kernel needs and stays there; a launch needing more grows it again.
+SGB_API int32_t gpu_stack_limit(uint64_t set_bytes, uint64_t *current) {
+    cudaError_t e = cudaSuccess;
+    if (set_bytes) e = cudaDeviceSetLimit(cudaLimitStackSize, (size_t)set_bytes);
+    size_t v = 0;
+    if (e == cudaSuccess && current) e = cudaDeviceGetLimit(&v, cudaLimitStackSize);
+    if (current) *current = v;
+    return (int32_t)e;
+}
+
 SGB_API int32_t gpu_kin_set_straggler_budget(uint32_t attempts) {
     g.straggler_budget = attempts;
     return 0;
