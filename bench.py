@@ -242,6 +242,16 @@ def cpu_baseline(cells_total: int, duration: float, seed: int, target_s: float, 
 
 # ---------------------------------------------------------------------------
 
+def stack_reservation() -> int:
+    """The context's per-thread local-memory reservation (the module fixes it at gpu_init)."""
+    import ctypes as C
+
+    import simstack_gb300 as sg
+    v = C.c_uint64()
+    sg.lib().gpu_stack_limit(0, C.byref(v))
+    return int(v.value)
+
+
 def air_workload(cells: int, duration: float) -> str:
     return (f"shipped 17-species humid-air mechanism, {cells} cells x {duration:g} s, Rodas3 rtol 1e-4 "
             f"atol 1e-12 mol/L, seeded log-uniform initial states")
@@ -432,7 +442,8 @@ def run_ours(args):
                    "cells_per_gpu": cells, "duration_s": args.duration, "precision": head,
                    "l2": "inputs larger than L2 (zone block %.0f MB per GPU)" % (block_bytes / 1e6),
                    "kernel": "persistent work-queue kernel (CTA-synchronous), autotuned launch shape",
-                   "tuning": tuned, "parallelism": f"replicas x{world} (cells partitioned, no collective)"},
+                   "tuning": tuned, "parallelism": f"replicas x{world} (cells partitioned, no collective)",
+                   "stack_reservation_bytes": stack_reservation()},
         "fp64": {"value": v64, "ms_per_step": ms_step64, "kernel_ms": ms64,
                  "parity": "bit-identical to the reference CPU solver (tests/test_gpu_parity.py)"},
         "mixed": {"value": vmx, "ms_per_step": ms_stepmx, "kernel_ms": msmx, "speedup_vs_fp64": v64 and vmx / v64,

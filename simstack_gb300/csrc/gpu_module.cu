@@ -34,6 +34,14 @@ cudaError_t launch_air_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
 cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
+cudaError_t local_air_p0(uint32_t, uint32_t, size_t *);
+cudaError_t local_air_p1(uint32_t, uint32_t, size_t *);
+cudaError_t local_air_p2(uint32_t, uint32_t, size_t *);
+cudaError_t local_air_p3(uint32_t, uint32_t, size_t *);
+cudaError_t local_table_p0(uint32_t, size_t *);
+cudaError_t local_table_p1(uint32_t, size_t *);
+cudaError_t local_table_p2(uint32_t, size_t *);
+cudaError_t local_table_p3(uint32_t, size_t *);
 uint64_t air_ops_signature();
 size_t coop_smem_bytes_for(int prec, const CoopMech &h);
 size_t coop_scratch_doubles_for(int prec, const CoopMech &h);
@@ -80,6 +88,12 @@ struct Module {
 };
 Module g;
 constexpr uint32_t kSuspendCap = 1u << 16;       // parked cells per launch
+// The context's per-thread stack (local memory) reservation, set once at gpu_init before any
+// launch so that it is never resized: the mixed kernel spills to local memory, and its speed
+// depends on where that memory lands (measured on GB300: 397-548 ms for the same launch at
+// different reservations and reallocations); 3,840 bytes covers every default-path kernel of
+// the shipped mechanism (the FP64 lanes need 3,680) and was the fastest such size measured.
+constexpr size_t kStackReserveBytes = 3840;
 constexpr uint32_t kResumeCtasPerSm = 8;         // cooperative CTAs per SM for parked cells
 
 
@@ -124,6 +138,18 @@ cudaError_t occupancy(uint32_t prec, const GpuKinTuning &t, int *blocks) {
 }
 
 cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A);
+
+// Local memory per thread the kernel of (precision, tuning) needs.
+cudaError_t local_bytes(uint32_t prec, const GpuKinTuning &t, size_t *bytes) {
+    const bool df = prec == 2 && g.mixed_variant == 1;
+    if (g.generated) {
+        if (df) return local_air_p3(t.kind, t.variant, bytes);
+        return prec == 0 ? local_air_p0(t.kind, t.variant, bytes) : prec == 1 ? local_air_p1(t.kind, t.variant, bytes)
+                                                                              : local_air_p2(t.kind, t.variant, bytes);
+    }
+    if (df) return local_table_p3(t.kind, bytes);
+    return prec == 0 ? local_table_p0(t.kind, bytes) : prec == 1 ? local_table_p1(t.kind, bytes) : local_table_p2(t.kind, bytes);
+}
 
 // Launches one advance of `A` with tuning `t` on the module stream; with a
 // straggler budget (precision 0), cells still stepping after that many
@@ -293,6 +319,11 @@ SGB_API int32_t gpu_init(uint32_t device_index, uint64_t arena_bytes, GpuInfo *i
         cudaEventCreate(&g.async_begin);
         cudaEventCreate(&g.async_end);
         cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking);
+    }
+    size_t stack = 0;
+    if (cudaDeviceGetLimit(&stack, cudaLimitStackSize) == cudaSuccess && stack != kStackReserveBytes) {
+        e = cudaDeviceSetLimit(cudaLimitStackSize, kStackReserveBytes);
+        if (e != cudaSuccess) return (int32_t)e;
     }
     g.device = (int)device_index;
     g.sms = prop.multiProcessorCount;
@@ -520,12 +551,23 @@ SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuK
     winner.ms = 1e30f;
     const Cand *list = kind == 2 ? sync_cands : cands;
     const size_t count = kind == 2 ? sizeof(sync_cands) / sizeof(Cand) : sizeof(cands) / sizeof(Cand);
+    // candidates that would grow the context's stack reservation are skipped, unless none fits
+    size_t have = 0, least = (size_t)-1;
+    cudaDeviceGetLimit(&have, cudaLimitStackSize);
+    for (size_t ci = 0; ci < count; ++ci) {
+        GpuKinTuning t = {kind, list[ci].block, list[ci].ctas, list[ci].variant, 0.0f};
+        size_t need = 0;
+        if (local_bytes(launch->precision, t, &need) == cudaSuccess && need < least) least = need;
+    }
+    const bool keep_reservation = least <= have;
     for (size_t ci = 0; ci < count; ++ci) {
         const Cand &c = list[ci];
         if (e != cudaSuccess) break;
         if (kind == 0 && c.ctas != 0) continue;
         {
             GpuKinTuning t = {kind, c.block, c.ctas, c.variant, 0.0f};
+            size_t need = 0;
+            if (keep_reservation && local_bytes(launch->precision, t, &need) == cudaSuccess && need > have) continue;
             float ms = 0.0f, best_ms = 1e30f;
             for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {   // the faster of two runs
                 e = advance_sync(launch, t, &ms);

@@ -24,6 +24,10 @@ cudaError_t SGB_CAT(occupancy_air_p, SGB_PREC)(uint32_t kind, uint32_t variant, 
     return occupancy_one<GenOps<AirOps>, Rodas3Coef, SGB_PREC>(kind, variant, block, 0, blocks_per_sm);
 }
 
+cudaError_t SGB_CAT(local_air_p, SGB_PREC)(uint32_t kind, uint32_t variant, size_t *bytes) {
+    return local_bytes_one<GenOps<AirOps>, Rodas3Coef, SGB_PREC>(kind, variant, bytes);
+}
+
 }   // namespace sgb
 
 #if SGB_PREC == 0

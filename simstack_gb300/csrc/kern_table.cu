@@ -23,4 +23,8 @@ cudaError_t SGB_CAT(occupancy_table_p, SGB_PREC)(uint32_t kind, uint32_t block, 
     return occupancy_one<TableOps, RuntimeCoef, SGB_PREC, 1>(kind, 0, block, smem, blocks_per_sm);
 }
 
+cudaError_t SGB_CAT(local_table_p, SGB_PREC)(uint32_t kind, size_t *bytes) {
+    return local_bytes_one<TableOps, RuntimeCoef, SGB_PREC, 1>(kind, 0, bytes);
+}
+
 }   // namespace sgb

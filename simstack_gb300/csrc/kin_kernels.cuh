@@ -199,6 +199,15 @@ cudaError_t launch_one(const Shape &s, const DevArgs &A, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
+// Local memory (stack frame) a kernel variant needs per thread.
+template <class Ops, class M, int PREC, int kVariants = 2>
+cudaError_t local_bytes_one(uint32_t kind, uint32_t variant, size_t *bytes) {
+    cudaFuncAttributes attr;
+    cudaError_t e = cudaFuncGetAttributes(&attr, kernel_for<Ops, M, PREC, kVariants>(kind, variant));
+    *bytes = e == cudaSuccess ? attr.localSizeBytes : 0;
+    return e;
+}
+
 template <class Ops, class M, int PREC, int kVariants = 2>
 cudaError_t occupancy_one(uint32_t kind, uint32_t variant, uint32_t block, size_t smem, int *blocks_per_sm) {
     void (*fn)(DevArgs) = kernel_for<Ops, M, PREC, kVariants>(kind, variant);
