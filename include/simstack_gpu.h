@@ -285,6 +285,10 @@ SGB_API int32_t gpu_kin_coop_info(uint64_t *out);
  * multiple of 32) and resident CTAs per SM (1..2; capped by occupancy). Defaults: FP64 256 x 2,
  * mixed 512 x 1 (its FP32 LU fills one SM's shared memory). */
 SGB_API int32_t gpu_kin_coop_set_shape(uint32_t precision, uint32_t block, uint32_t ctas_per_sm);
+/* Clock cycles per phase of the cooperative kernel (rhs, Jacobian, factor, solves, -, whole
+ * attempts), summed over CTAs' thread 0, in a build with -DSGB_COOP_PROFILE (zeros otherwise);
+ * reading resets them. */
+SGB_API int32_t gpu_kin_coop_phase_cycles(uint64_t *out6);
 /* Refinement sweeps per stage solve of the mixed cooperative path (1..4, default 1). */
 SGB_API int32_t gpu_kin_coop_set_refinement(uint32_t sweeps);
 

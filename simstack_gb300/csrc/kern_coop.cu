@@ -59,6 +59,21 @@ struct CoopTab {
     }
 };
 
+// Build-time phase timing (-DSGB_COOP_PROFILE): thread 0 of every CTA adds the
+// clock cycles of each phase to g_coop_phase_cycles (rhs, Jacobian, factor,
+// solves, refinement residual, total attempt).
+#ifdef SGB_COOP_PROFILE
+__device__ unsigned long long g_coop_phase_cycles[8];
+#define SGB_PHASE(i, stmt)                                                      \
+    do {                                                                        \
+        const long long _t0 = clock64();                                       \
+        stmt;                                                                   \
+        if (tid == 0) atomicAdd(&g_coop_phase_cycles[i], (unsigned long long)(clock64() - _t0)); \
+    } while (0)
+#else
+#define SGB_PHASE(i, stmt) stmt
+#endif
+
 // Shared-memory doubles before the mixed path's FP32 arrays.
 __host__ __device__ inline uint32_t coop_smem_doubles(uint32_t n, uint32_t R) { return 11u * n + 2u * R + 8u; }
 
@@ -345,7 +360,7 @@ struct CoopCell {
         float *xs = x32;
         for (uint32_t s = tid; s < n; s += NT) xs[s] = (float)rb[s];
         sync();
-        solve(xs);
+        SGB_PHASE(3, solve(xs));
         for (uint32_t s = tid; s < n; s += NT) out[s] = (double)xs[s];
         sync();
         for (uint32_t sw = 0; sw < A.ir_sweeps; ++sw) {
@@ -355,7 +370,7 @@ struct CoopCell {
                 xs[i] = (float)(rb[i] - w);
             }
             sync();
-            solve(xs);
+            SGB_PHASE(3, solve(xs));
             for (uint32_t s = tid; s < n; s += NT) out[s] = out[s] + (double)xs[s];
             sync();
         }
@@ -376,10 +391,10 @@ struct CoopCell {
             red[2] = 1.0 / (hs * M::gamma0(A));
             red[3] = 1.0 / hs;
         }
-        rhs(y);
-        neg_jac(y);
+        SGB_PHASE(0, rhs(y));
+        SGB_PHASE(1, neg_jac(y));
         const double ghinv = red[2];
-        factor((Cf)ghinv);
+        SGB_PHASE(2, factor((Cf)ghinv));
         const double hinv = red[3];
 
         bool fcn_at_y = true;
@@ -402,7 +417,7 @@ struct CoopCell {
                         ytmp[s] = v;
                     }
                     sync();
-                    rhs(ytmp);
+                    SGB_PHASE(0, rhs(ytmp));
                     fcn_at_y = !moved;
                 }
             }
@@ -420,7 +435,7 @@ struct CoopCell {
             if constexpr (kMixed) {
                 solve_refined(A, ghinv, Ks);
             } else {
-                solve(Ks);
+                SGB_PHASE(3, solve(Ks));
             }
         }
 
@@ -544,7 +559,15 @@ __global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant_
             if (idx >= A.lanes) break;
             C.load(A, cell);
         }
-        while (C.settle(A, cell)) C.attempt(A);
+        while (C.settle(A, cell)) {
+            const long long t_attempt = clock64();
+            C.attempt(A);
+#ifdef SGB_COOP_PROFILE
+            if (threadIdx.x == 0) atomicAdd(&g_coop_phase_cycles[5], (unsigned long long)(clock64() - t_attempt));
+#else
+            (void)t_attempt;
+#endif
+        }
         C.store(A, cell);
     }
 }
@@ -735,6 +758,22 @@ SGB_API int32_t gpu_kin_coop_info(uint64_t *out8) {
     const CoopMech &h = cm.head;
     out8[0] = h.n; out8[1] = h.R; out8[2] = h.nnz; out8[3] = h.nj;
     out8[4] = h.l_entries; out8[5] = h.u_entries; out8[6] = h.lu_updates; out8[7] = h.bytes;
+    return 0;
+}
+
+// Phase cycle counters of a -DSGB_COOP_PROFILE build (zeros otherwise); reading resets them.
+SGB_API int32_t gpu_kin_coop_phase_cycles(uint64_t *out6) {
+    if (!out6) return (int32_t)cudaErrorInvalidValue;
+    memset(out6, 0, 6 * sizeof(uint64_t));
+#ifdef SGB_COOP_PROFILE
+    unsigned long long v[8];
+    cudaError_t e = cudaMemcpyFromSymbol(v, g_coop_phase_cycles, sizeof(v));
+    if (e != cudaSuccess) return (int32_t)e;
+    for (int i = 0; i < 6; ++i) out6[i] = v[i];
+    memset(v, 0, sizeof(v));
+    e = cudaMemcpyToSymbol(g_coop_phase_cycles, v, sizeof(v));
+    if (e != cudaSuccess) return (int32_t)e;
+#endif
     return 0;
 }
 
