@@ -289,7 +289,7 @@ SGB_API int32_t gpu_kin_coop_set_shape(uint32_t precision, uint32_t block, uint3
  * attempts), summed over CTAs' thread 0, in a build with -DSGB_COOP_PROFILE (zeros otherwise);
  * reading resets them. */
 SGB_API int32_t gpu_kin_coop_phase_cycles(uint64_t *out6);
-/* Refinement sweeps per stage solve of the mixed cooperative path (1..4, default 1). */
+/* Refinement sweeps per stage solve of the mixed cooperative path (0..4, default 1). */
 SGB_API int32_t gpu_kin_coop_set_refinement(uint32_t sweeps);
 
 /* ---------------------------------------------------------------------------

@@ -246,20 +246,34 @@ struct CoopCell {
     __device__ void factor(Cf ghinv) {
         for (uint32_t k = 0; k < n; ++k) {
             const uint32_t nl = lcnt[k];
-            // 1/U(k,k) once (a division costs many FP64 instructions per warp), shared through red[4]
-            Cf *inv_s = (Cf *)(red + 4);
-            if (tid == 0) {
-                const Cf inv = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
-                a[(size_t)k * ld + k] = inv;
-                *inv_s = inv;
+            Cf inv;
+            if constexpr (kMixed) {
+                // FP32: every thread divides (cheap on the FP32 pipe); the inverted diagonal is
+                // stored after the barrier below, once every thread has read a[k][k]
+                if (nl == 0) {   // nothing below the pivot: the next pivot reads none of this pivot's writes
+                    if (tid == 0) a[(size_t)k * ld + k] = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
+                    continue;
+                }
+                inv = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
+            } else {
+                // FP64: 1/U(k,k) once (a division costs many FP64 instructions per warp), shared through red[4]
+                Cf *inv_s = (Cf *)(red + 4);
+                if (tid == 0) {
+                    const Cf v = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
+                    a[(size_t)k * ld + k] = v;
+                    *inv_s = v;
+                }
+                if (nl == 0) continue;
+                sync();
+                inv = *inv_s;
             }
-            if (nl == 0) continue;   // nothing below the pivot: the next pivot reads none of this pivot's writes
-            sync();
-            const Cf inv = *inv_s;
             // L column k: l_i = a[i][k] / U(k,k)
             for (uint32_t i = k + 1 + tid; i < n; i += NT)
                 if (bit(i, k)) a[(size_t)i * ld + k] = a[(size_t)i * ld + k] * inv;
             sync();
+            if constexpr (kMixed) {
+                if (tid == 0) a[(size_t)k * ld + k] = inv;
+            }
             // pivot row k (final) cached per lane: columns k+1+lane+32c in the pattern
             const uint32_t width = n - 1 - k, chunks = (width + 31) / 32;
             Cf pv[kCoopMaxCols];
@@ -787,7 +801,7 @@ SGB_API int32_t gpu_kin_coop_set_shape(uint32_t precision, uint32_t block, uint3
 }
 
 SGB_API int32_t gpu_kin_coop_set_refinement(uint32_t sweeps) {
-    if (sweeps < 1 || sweeps > 4) return (int32_t)cudaErrorInvalidValue;
+    if (sweeps > 4) return (int32_t)cudaErrorInvalidValue;
     cm.ir_sweeps = sweeps;
     return 0;
 }
