@@ -13,10 +13,14 @@
  *
  * New capability is added as extra exports, never by changing a reference
  * signature:
- *   - GpuKinLaunch.precision = 2: mixed precision (FP32 RHS, Jacobian and LU,
- *     FP64 iterative-refinement residual, FP64 state and step control)
+ *   - GpuKinLaunch.precision = 2: mixed precision (default: double-float state
+ *     with FP32 Jacobian, LU and solves; or FP64 state with an FP64-residual
+ *     refinement sweep, gpu_kin_set_mixed_variant)
  *   - gpu_kin_advance_queue: persistent kernel over a device work queue
  *   - gpu_kin_autotune / gpu_kin_get_tuning: launch-shape autotuner
+ *   - gpu_kin_set_straggler_budget: FP64 straggler hand-off to the cooperative kernel
+ *   - gpu_kin_coop_*: cooperative (one CTA per cell) kernels for large mechanisms
+ *   - gpu_advect, gpu_serve_*: film advection, CUDA-graph coupling step, serving
  *   - kin_model_*: host-side mechanism compiler (the reference's kin_build.cpp)
  *
  * No torch types, no CUDA types: plain pointers and sizes. Device pointers are

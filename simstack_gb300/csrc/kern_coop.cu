@@ -320,8 +320,9 @@ struct CoopCell {
                 const Cf *row = a + (size_t)(i < n ? i : 0) * ld;
                 // this row's pattern bits for the block's columns, below the diagonal only
                 const uint32_t w = i < n ? pat[i * 8u + b] & ((1u << lane) - 1u) : 0u;
+                const uint32_t kn = kend - kb;   // columns in this block (32, or fewer in the last)
 #pragma unroll 8
-                for (uint32_t kk = 0; kk < 32; ++kk) {
+                for (uint32_t kk = 0; kk < kn; ++kk) {
                     const V xk = __shfl_sync(0xffffffffu, xi, kk);
                     if ((w >> kk) & 1u) xi = sgb_fma(-(V)row[kb + kk], xk, xi);
                 }
@@ -349,7 +350,7 @@ struct CoopCell {
                 const uint32_t w = i < n ? pat[i * 8u + b] & ~((2u << lane) - 1u) : 0u;
                 const V d = i < n ? (V)row[i] : (V)0.0;   // 1/U(i,i)
 #pragma unroll 8
-                for (uint32_t kk = 32; kk-- > 0;) {
+                for (uint32_t kk = kend - kb; kk-- > 0;) {
                     if (lane == kk) xi = xi * d;   // row kb+kk: all its updates are in
                     const V xk = __shfl_sync(0xffffffffu, xi, kk);
                     if ((w >> kk) & 1u) xi = sgb_fma(-(V)row[kb + kk], xk, xi);
