@@ -286,8 +286,8 @@ SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *launch, float *kernel_m
 /* out[8]: n, R, LU non-zeros, Jacobian entries, L entries, U entries, LU updates, image bytes. */
 SGB_API int32_t gpu_kin_coop_info(uint64_t *out);
 /* Launch shape of the cooperative kernels per precision (0 or 2): threads per CTA (64..512,
- * multiple of 32) and resident CTAs per SM (1..2; capped by occupancy). Defaults: FP64 256 x 2,
- * mixed 512 x 1 (its FP32 LU fills one SM's shared memory). */
+ * multiple of 32) and resident CTAs per SM (1..2; capped by occupancy). Defaults: 512 x 1 for
+ * both (measured fastest for FP64 on 200 species; the mixed FP32 LU fills one SM's shared memory). */
 SGB_API int32_t gpu_kin_coop_set_shape(uint32_t precision, uint32_t block, uint32_t ctas_per_sm);
 /* Clock cycles per phase of the cooperative kernel (rhs, Jacobian, factor, solves, -, whole
  * attempts), summed over CTAs' thread 0, in a build with -DSGB_COOP_PROFILE (zeros otherwise);

@@ -404,14 +404,14 @@ SGB_API int32_t gpu_kin_set_mech(const KinMech *mech, const KinMethod *method, c
     g.control = *control;
     g.generated = fnv1a(mech, sizeof(KinMech)) == air_ops_signature() && method_is_rodas3(method);
     g.have_mech = true;
-    // the cooperative image of the same mechanism, for the straggler hand-off
+    // the cooperative image of the same mechanism, for the straggler hand-off (none: no hand-off)
+    if (g.d_coop_image) cudaFree(g.d_coop_image);
+    if (g.d_coop_scratch) cudaFree(g.d_coop_scratch);
+    g.d_coop_image = nullptr;
+    g.d_coop_scratch = nullptr;
     std::vector<uint8_t> coop;
     if (coop_image(*mech, &coop)) {
         memcpy(&g.coop_head, coop.data(), sizeof(CoopMech));
-        if (g.d_coop_image) cudaFree(g.d_coop_image);
-        if (g.d_coop_scratch) cudaFree(g.d_coop_scratch);
-        g.d_coop_image = nullptr;
-        g.d_coop_scratch = nullptr;
         g.coop_grid = (uint32_t)g.sms * kResumeCtasPerSm;
         const size_t a = coop_scratch_doubles_for(0, g.coop_head), b = coop_scratch_doubles_for(2, g.coop_head);
         e = cudaMalloc(&g.d_coop_image, coop.size());

@@ -601,8 +601,8 @@ struct CoopModule {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t ir_sweeps = 1;
     float last_ms = 0.0f;
-    uint32_t block[3] = {256, 0, 512};    // threads per CTA by precision (0 FP64, 2 mixed)
-    uint32_t ctas[3] = {2, 0, 1};         // resident CTAs per SM by precision
+    uint32_t block[3] = {512, 0, 512};    // threads per CTA by precision (0 FP64, 2 mixed)
+    uint32_t ctas[3] = {1, 0, 1};         // resident CTAs per SM by precision
     int sms = 0;
 };
 CoopModule cm;
