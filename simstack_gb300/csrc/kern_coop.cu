@@ -77,6 +77,26 @@ __device__ unsigned long long g_coop_phase_cycles[8];
 // Shared-memory doubles before the mixed path's FP32 arrays.
 __host__ __device__ inline uint32_t coop_smem_doubles(uint32_t n, uint32_t R) { return 11u * n + 2u * R + 8u; }
 
+constexpr size_t kCoopSmemBudget = 200 * 1024;   // the term lists join shared memory while the total stays below this
+
+// Shared memory of one CTA: doubles, x32 (256 floats), pattern (n x 8 words), lcnt (n u16,
+// padded), then the LU (mixed always, n x ld floats; FP64 when it fits kCoopSmemLuF64Max), then
+// -- when they fit the budget -- the RHS / Jacobian term lists (image bytes [off_reac, off_lbeg)).
+struct CoopSmemLayout {
+    size_t lu, lu_bytes, terms, terms_bytes, total;
+};
+__host__ __device__ inline CoopSmemLayout coop_layout(int prec, const CoopMech &h) {
+    CoopSmemLayout L;
+    L.lu = (size_t)coop_smem_doubles(h.n, h.R) * 8 + kCoopMaxSpecies * 4 + (size_t)h.n * 32 + ((h.n + 7) / 8) * 16;
+    const size_t lu64 = (size_t)h.n * h.ld * sizeof(double);
+    L.lu_bytes = prec == 2 ? (size_t)h.n * h.ld * 4 : (lu64 <= kCoopSmemLuF64Max ? lu64 : 0);
+    L.terms = (L.lu + L.lu_bytes + 15) / 16 * 16;
+    const size_t tb = (size_t)h.off_lbeg - h.off_reac;
+    L.terms_bytes = L.terms + tb <= kCoopSmemBudget ? tb : 0;
+    L.total = L.terms + L.terms_bytes;
+    return L;
+}
+
 template <int PREC>
 struct CoopCell {
     typedef typename Pick<PREC == 0, double, float>::type Cf;   // LU and solve arithmetic
@@ -547,14 +567,30 @@ __global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant_
     }
     C.pat = pat_s;
     C.lcnt = lcnt_s;
+    const CoopSmemLayout lay = coop_layout(PREC, *C.tb.h);
+    unsigned char *smb = (unsigned char *)sm;
     double *g = scratch + (size_t)blockIdx.x * stride;
     if constexpr (PREC == 2) {
-        C.a = (typename CoopCell<PREC>::Cf *)(lcnt_s + ((n + 7) / 8) * 8);   // 16-byte aligned
+        C.a = (typename CoopCell<PREC>::Cf *)(smb + lay.lu);
         C.js = g;
     } else {   // FP64: small LUs in shared memory, large ones in per-CTA global scratch (L2)
-        const bool in_smem = (size_t)n * C.ld * sizeof(double) <= kCoopSmemLuF64Max;
-        C.a = in_smem ? (typename CoopCell<PREC>::Cf *)(lcnt_s + ((n + 7) / 8) * 8) : (typename CoopCell<PREC>::Cf *)g;
+        C.a = lay.lu_bytes ? (typename CoopCell<PREC>::Cf *)(smb + lay.lu) : (typename CoopCell<PREC>::Cf *)g;
         C.js = nullptr;
+    }
+    if (lay.terms_bytes) {   // the RHS / Jacobian term lists, once per CTA
+        const CoopMech *h = C.tb.h;
+        const uint4 *src = (const uint4 *)((const unsigned char *)A.tables + h->off_reac);
+        uint4 *dst = (uint4 *)(smb + lay.terms);
+        for (uint32_t q = threadIdx.x; q < lay.terms_bytes / 16; q += blockDim.x) dst[q] = src[q];
+        unsigned char *t = smb + lay.terms - h->off_reac;   // image offset o lives at t + o
+        C.tb.reac = (const uint16_t *)(t + h->off_reac);
+        C.tb.fbeg = (const uint32_t *)(t + h->off_fbeg);
+        C.tb.fent = (const CoopTerm *)(t + h->off_fent);
+        C.tb.jbeg = (const uint32_t *)(t + h->off_jbeg);
+        C.tb.jent = (const CoopTerm *)(t + h->off_jent);
+        C.tb.jpos = (const uint32_t *)(t + h->off_jpos);
+        C.tb.jrow = (const uint32_t *)(t + h->off_jrow);
+        C.tb.jcol = (const uint16_t *)(t + h->off_jcol);
     }
     __syncthreads();
     const uint32_t parked = A.resume ? min(*(volatile uint32_t *)A.suspend_count, A.suspend_cap) : 0u;
@@ -608,15 +644,7 @@ struct CoopModule {
 CoopModule cm;
 constexpr uint32_t kCoopMaxCtasPerSm = 2;   // scratch slots per SM
 
-// Shared memory: doubles, x32 (256 floats), pattern (n x 8 words), lcnt (n u16, padded), then the LU:
-// mixed always (n x ld floats), FP64 when it fits kCoopSmemLuF64Max (n x ld doubles).
-size_t coop_smem_bytes(int prec, const CoopMech &h) {
-    size_t b = (size_t)coop_smem_doubles(h.n, h.R) * 8 + kCoopMaxSpecies * 4 + (size_t)h.n * 32 + ((h.n + 7) / 8) * 16;
-    const size_t lu64 = (size_t)h.n * h.ld * sizeof(double);
-    if (prec == 2) b += (size_t)h.n * h.ld * 4;
-    else if (lu64 <= kCoopSmemLuF64Max) b += lu64;
-    return b;
-}
+size_t coop_smem_bytes(int prec, const CoopMech &h) { return coop_layout(prec, h).total; }
 
 size_t coop_scratch_doubles(int prec, const CoopMech &h) {
     size_t d = prec == 2 ? (size_t)h.nj : (size_t)h.n * h.ld;
