@@ -308,29 +308,14 @@ struct CoopCell {
                     live |= 1u << c;
                 }
             }
-            // two rows per warp at a time, every load issued before any store (the updates of
-            // different elements are independent; this only lets their memory latencies overlap)
-            for (uint32_t i0 = k + 1 + warp; i0 < n; i0 += 2 * W) {
-                const uint32_t i1 = i0 + W;
-                const bool r0 = bit(i0, k), r1 = i1 < n && bit(i1, k);   // same for the whole warp
-                if (!r0 && !r1) continue;
-                Cf *row0 = a + (size_t)i0 * ld, *row1 = a + (size_t)(r1 ? i1 : i0) * ld;
-                const uint32_t m0 = r0 ? live : 0u, m1 = r1 ? live : 0u;
-                const Cf l0 = r0 ? row0[k] : (Cf)0.0, l1 = r1 ? row1[k] : (Cf)0.0;
-                Cf v0[kCoopMaxCols], v1[kCoopMaxCols];
+            for (uint32_t i = k + 1 + warp; i < n; i += W) {
+                if (!bit(i, k)) continue;   // same for the whole warp
+                Cf *row = a + (size_t)i * ld;
+                const Cf l = row[k];
 #pragma unroll
                 for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
                     const uint32_t j = k + 1 + lane + 32u * c;
-                    v0[c] = (Cf)0.0;
-                    v1[c] = (Cf)0.0;
-                    if ((m0 >> c) & 1u) v0[c] = row0[j];
-                    if ((m1 >> c) & 1u) v1[c] = row1[j];
-                }
-#pragma unroll
-                for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
-                    const uint32_t j = k + 1 + lane + 32u * c;
-                    if ((m0 >> c) & 1u) row0[j] = sgb_fma(-l0, pv[c], v0[c]);
-                    if ((m1 >> c) & 1u) row1[j] = sgb_fma(-l1, pv[c], v1[c]);
+                    if ((live >> c) & 1u) row[j] = sgb_fma(-l, pv[c], row[j]);
                 }
             }
             sync();
