@@ -59,6 +59,8 @@ def parse():
                          "config4: 200-species / 1,200-reaction synthetic mechanism, one CTA per cell; "
                          "config5: served requests (Poisson arrivals) with film advection, p50/p99 latency")
     ap.add_argument("--requests", type=int, default=48, help="config5: requests in the served sample")
+    ap.add_argument("--tuning", default=None,
+                    help="--profile-case: launch shape block,variant,ctas_per_sm of the CTA-synchronous queue kernel")
     ap.add_argument("--mixed-variant", type=int, choices=[0, 1], default=None,
                     help="--profile-case mixed: 0 = FP64 state with refinement, 1 = double-float state (default)")
     ap.add_argument("--fp64-cells", type=int, default=1216,
@@ -766,6 +768,9 @@ def run_profile_case(args):
     mod = sg.Module(0, 2 * sg.ZoneBlock(17, 44, args.cells).nbytes + (64 << 20))
     if args.mixed_variant is not None:
         mod.set_mixed_variant(args.mixed_variant)
+    if args.tuning:
+        block, variant, ctas = (int(v) for v in args.tuning.split(","))
+        mod.set_tuning(kind=2, block=block, variant=variant, ctas_per_sm=ctas)
     ctl = sg.control() if prec != 1 else sg.control(rtol=1e-3, atol=1e8, max_steps=20000)
     mod.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), ctl)
     z = sg.air_cells(args.cells, seed=args.seed)
