@@ -758,10 +758,16 @@ def run_profile_case(args):
         z = sg.synthetic_cells(pm, args.cells, seed=args.seed + 1)
         mod = sg.Module(0, 2 * z.nbytes + (64 << 20))
         mod.coop_set_mech(pm, sg.method("rodas3"), sg.control(rtol=1e-4, atol=1e-12, max_steps=200000))
+        import ctypes as C
+        phases = (C.c_uint64 * 6)()
+        sg.lib().gpu_kin_coop_phase_cycles(phases)   # reset (a build with -DSGB_COOP_PROFILE counts)
         ms = mod.coop_integrate(z, args.duration, precision=prec)
+        sg.lib().gpu_kin_coop_phase_cycles(phases)
         steps = float(z["steps"][:args.cells].sum() + z["rejects"][:args.cells].sum())
+        names = ("rhs", "jacobian", "factor", "solves", "unused", "attempt")
         print(json.dumps({"case": args.profile_case, "cells": args.cells, "duration_s": args.duration, "kernel_ms": ms,
-                          "cell_steps": steps}))
+                          "cell_steps": steps,
+                          "cycles_per_cell_step_thread0": {k: round(v / steps) for k, v in zip(names, phases) if k != "unused"}}))
         return
 
     prec = {"f64": 0, "f32": 1, "mixed": 2}[args.profile_case]
