@@ -273,3 +273,60 @@ def test_zero_duration_and_empty(module, oracle_lib):
     module.integrate(z, 0.0, precision=0)
     oracle_run(oracle_lib, ref, 0.0)
     assert_bits(z, ref)
+
+
+def test_table_path_near_capacity(module, oracle_lib):
+    """A synthetic mechanism near the KinMech capacities (32 species, 64 reactions,
+    477 of 512 LU non-zeros, 1,769 updates) through the table-driven kernels:
+    FP64 bit for bit against the oracle, the mixed path against its model."""
+    pm = sg.Model.synthetic(seed=1, species=32, reactions=64, bimolecular=0.7, products=1)
+    om = oracle_lib.Mechanism()
+    for s in range(32):
+        om.add_species(f"S{s}", True)
+    for r in range(pm.R):
+        om.add_reaction(sg.model_equation(pm, r), "arr", (float(pm.k_const[r]), 0.0, 0.0))
+    om.finalize()
+    ctl = dict(rtol=1e-4, atol=1e-12, max_steps=200000)
+    module.set_mech(pm.kinmech(), sg.method("rodas3"), sg.control(**ctl))
+    assert pm.counts()["nnz"] == 477
+    z = sg.synthetic_cells(pm, 256, seed=3)
+    ref = z.copy()
+    module.integrate(z, 1.0, precision=0)
+    om.advance("rodas3", oracle_lib.control(**ctl), ref.as_dict(), ref.padded, 0, ref.padded, 1.0, 0, 0)
+    assert_bits(z, ref)
+    zm = sg.synthetic_cells(pm, 256, seed=3)
+    refm = zm.copy()
+    module.integrate(zm, 1.0, precision=2)
+    oracle_lib.advance_mixed(om, "rodas3", oracle_lib.control(**ctl), refm.as_dict(), refm.padded, 0, refm.padded, 1.0,
+                             sweeps=1, variant=module.mixed_variant())
+    assert_bits(zm, refm)
+    module.reset_arena()
+
+
+def test_full_size_sampled_cells(module, oracle_lib):
+    """The full 1,048,576-cell x 10 s workload on the GPU; 256 cells sampled across
+    the batch checked against the oracle (cells are independent): FP64 bit for bit,
+    mixed within its bounds."""
+    module.reset_arena()
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    cells = 1 << 20
+    z = sg.air_cells(cells, seed=1)
+    pick = np.sort(np.random.default_rng(5).choice(cells, size=256, replace=False))
+    zs = sg.ZoneBlock(17, 44, 256)
+    for name in sg.ROWS_ORDER:
+        zs[name][...] = z[name][..., pick]
+    base = module.alloc(z.nbytes)
+    out = {}
+    for prec in (0, 2):
+        w = z.copy()
+        module.integrate(w, 10.0, precision=prec, device_base=base)
+        out[prec] = w
+    ref = zs.copy()
+    oracle_run(oracle_lib, ref, 10.0)
+    for name in STATE:
+        assert out[0][name][..., pick].tobytes() == np.ascontiguousarray(ref[name]).tobytes(), name
+    got = sg.ZoneBlock(17, 44, 256)
+    got["y"][...] = out[2]["y"][:, pick]
+    sig, floored = mixed_errors(got, ref)
+    assert np.quantile(sig, 0.99) < 1e-6 and out[2]["failed"].max() == 0.0
+    module.reset_arena()
