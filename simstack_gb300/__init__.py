@@ -171,6 +171,7 @@ def lib() -> C.CDLL:
             "gpu_kin_coop_info": (i32, [C.POINTER(u64)]),
             "gpu_kin_coop_set_refinement": (i32, [u32]),
             "gpu_kin_coop_set_shape": (i32, [u32, u32, u32]),
+            "gpu_kin_coop_set_smem_budget": (i32, [u32, u32]),
             "gpu_kin_coop_phase_cycles": (i32, [C.POINTER(u64)]),
             "gpu_advect": (i32, [vp, u32, u32, u32, u32, vp, d, u32, vp]),
             "gpu_serve_open": (i32, [u64, C.POINTER(KinControl)]),

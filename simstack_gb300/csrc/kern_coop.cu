@@ -77,7 +77,7 @@ __device__ unsigned long long g_coop_phase_cycles[8];
 // Shared-memory doubles before the mixed path's FP32 arrays.
 __host__ __device__ inline uint32_t coop_smem_doubles(uint32_t n, uint32_t R) { return 11u * n + 2u * R + 8u; }
 
-constexpr size_t kCoopSmemBudget = 200 * 1024;   // the term lists join shared memory while the total stays below this
+constexpr uint32_t kCoopSmemBudget = 200 * 1024;   // default: the term lists join shared memory while the total stays below this
 
 // Shared memory of one CTA: doubles, x32 (256 floats), pattern (n x 8 words), lcnt (n u16,
 // padded), then the LU (mixed always, n x ld floats; FP64 when it fits kCoopSmemLuF64Max), then
@@ -85,14 +85,14 @@ constexpr size_t kCoopSmemBudget = 200 * 1024;   // the term lists join shared m
 struct CoopSmemLayout {
     size_t lu, lu_bytes, terms, terms_bytes, total;
 };
-__host__ __device__ inline CoopSmemLayout coop_layout(int prec, const CoopMech &h) {
+__host__ __device__ inline CoopSmemLayout coop_layout(int prec, const CoopMech &h, uint32_t budget) {
     CoopSmemLayout L;
     L.lu = (size_t)coop_smem_doubles(h.n, h.R) * 8 + kCoopMaxSpecies * 4 + (size_t)h.n * 32 + ((h.n + 7) / 8) * 16;
     const size_t lu64 = (size_t)h.n * h.ld * sizeof(double);
     L.lu_bytes = prec == 2 ? (size_t)h.n * h.ld * 4 : (lu64 <= kCoopSmemLuF64Max ? lu64 : 0);
     L.terms = (L.lu + L.lu_bytes + 15) / 16 * 16;
     const size_t tb = (size_t)h.off_lbeg - h.off_reac;
-    L.terms_bytes = L.terms + tb <= kCoopSmemBudget ? tb : 0;
+    L.terms_bytes = L.terms + tb <= budget ? tb : 0;
     L.total = L.terms + L.terms_bytes;
     return L;
 }
@@ -567,7 +567,7 @@ __global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant_
     }
     C.pat = pat_s;
     C.lcnt = lcnt_s;
-    const CoopSmemLayout lay = coop_layout(PREC, *C.tb.h);
+    const CoopSmemLayout lay = coop_layout(PREC, *C.tb.h, A.coop_smem_budget);
     unsigned char *smb = (unsigned char *)sm;
     double *g = scratch + (size_t)blockIdx.x * stride;
     if constexpr (PREC == 2) {
@@ -639,12 +639,15 @@ struct CoopModule {
     float last_ms = 0.0f;
     uint32_t block[3] = {512, 0, 512};    // threads per CTA by precision (0 FP64, 2 mixed)
     uint32_t ctas[3] = {1, 0, 1};         // resident CTAs per SM by precision
+    uint32_t smem_budget[3] = {kCoopSmemBudget, 0, kCoopSmemBudget};
     int sms = 0;
 };
 CoopModule cm;
 constexpr uint32_t kCoopMaxCtasPerSm = 2;   // scratch slots per SM
 
-size_t coop_smem_bytes(int prec, const CoopMech &h) { return coop_layout(prec, h).total; }
+size_t coop_smem_bytes(int prec, const CoopMech &h, uint32_t budget = kCoopSmemBudget) {
+    return coop_layout(prec, h, budget).total;
+}
 
 size_t coop_scratch_doubles(int prec, const CoopMech &h) {
     size_t d = prec == 2 ? (size_t)h.nj : (size_t)h.n * h.ld;
@@ -659,10 +662,12 @@ size_t coop_scratch_doubles_for(int prec, const CoopMech &h) { return coop_scrat
 // The cooperative kernel on `A` (A.tables the coop image, A.cursor zeroed):
 // lanes [0, A.lanes), or with A.resume the cells a lane kernel parked;
 // `scratch` holds grid slots of coop_scratch_doubles_for(prec) doubles.
-cudaError_t coop_launch(int prec, const DevArgs &A, const CoopMech &head, double *scratch, uint32_t grid,
+cudaError_t coop_launch(int prec, const DevArgs &A0, const CoopMech &head, double *scratch, uint32_t grid,
                                uint32_t block, cudaStream_t s) {
     void (*fn)(DevArgs, double *, uint64_t) = prec == 0 ? kin_coop_kernel<0> : kin_coop_kernel<2>;
-    const size_t smem = coop_smem_bytes(prec, head);
+    DevArgs A = A0;
+    if (!A.coop_smem_budget) A.coop_smem_budget = kCoopSmemBudget;
+    const size_t smem = coop_smem_bytes(prec, head, A.coop_smem_budget);
     if (smem > 48 * 1024) {
         cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
@@ -735,7 +740,7 @@ SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *L, float *kernel_ms) {
     const int prec = (int)L->precision;
     int max_smem = 0;
     if (cudaDeviceGetAttribute(&max_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, 0) != cudaSuccess ||
-        coop_smem_bytes(prec, cm.head) > (size_t)max_smem)
+        coop_smem_bytes(prec, cm.head, cm.smem_budget[prec]) > (size_t)max_smem)
         return (int32_t)cudaErrorInvalidValue;   // the mixed path's FP32 LU must fit one CTA's shared memory
     DevArgs A;
     memset(&A, 0, sizeof(A));
@@ -768,7 +773,8 @@ SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *L, float *kernel_ms) {
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return (int32_t)e;
     void (*fn)(DevArgs, double *, uint64_t) = prec == 0 ? kin_coop_kernel<0> : kin_coop_kernel<2>;
-    const size_t smem = coop_smem_bytes(prec, cm.head);
+    A.coop_smem_budget = cm.smem_budget[prec];
+    const size_t smem = coop_smem_bytes(prec, cm.head, A.coop_smem_budget);
     e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return (int32_t)e;
     int fit = 0;
@@ -817,6 +823,12 @@ SGB_API int32_t gpu_kin_coop_phase_cycles(uint64_t *out6) {
     e = cudaMemcpyToSymbol(g_coop_phase_cycles, v, sizeof(v));
     if (e != cudaSuccess) return (int32_t)e;
 #endif
+    return 0;
+}
+
+SGB_API int32_t gpu_kin_coop_set_smem_budget(uint32_t precision, uint32_t bytes) {
+    if ((precision != 0 && precision != 2) || bytes > 227 * 1024) return (int32_t)cudaErrorInvalidValue;
+    cm.smem_budget[precision] = bytes;
     return 0;
 }
 

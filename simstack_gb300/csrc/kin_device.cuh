@@ -143,6 +143,7 @@ struct DevArgs {
     uint32_t *suspend_count;
     struct SuspendRec *suspend;
     uint32_t resume;           // cooperative kernel: take cells from the suspension list
+    uint32_t coop_smem_budget; // cooperative kernel: shared-memory bytes the term lists may fill up to
 };
 
 // The scalar state of a parked cell (its y, h and counters are in the zone block).
