@@ -193,11 +193,12 @@ def flops_per_step(model) -> dict:
 
 
 # DRAM bytes (read + write) per attempted cell-step of the queue kernels, from one ncu capture each
-# (262,144 cells x 0.5 s, `bench.py --profile-case f64|mixed`, default tuning; summaries in
-# profiles/kin_queue_cta_f64_air_262144x0.5s.txt and profiles/kin_queue_cta_mixed_df_air_262144x0.5s.txt).
+# (262,144 cells x 0.5 s, `bench.py --profile-case f64|mixed`; FP64 with the default tuning, mixed with the
+# shape the autotuner picks for the benchmark, 256 threads x 1 CTA/SM; summaries in
+# profiles/kin_queue_cta_f64_air_262144x0.5s.txt and profiles/kin_queue_cta_mixed_df_256thr_air_262144x0.5s.txt).
 # Nearly all of it is local-memory spill traffic, which grows with the cell-steps a launch executes;
 # the bench scales it to its own launch.
-DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 1916.1}
+DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 2045.3}
 
 
 def hbm_bytes_per_cell(n: int, R: int) -> int:
