@@ -290,7 +290,7 @@ SGB_API int32_t gpu_kin_coop_info(uint64_t *out);
  * both (measured fastest for FP64 on 200 species; the mixed FP32 LU fills one SM's shared memory). */
 SGB_API int32_t gpu_kin_coop_set_shape(uint32_t precision, uint32_t block, uint32_t ctas_per_sm);
 /* Shared-memory bytes per CTA up to which the cooperative kernel also stages the RHS / Jacobian term
- * lists (precision 0 or 2; default 200 KiB, 0 = never). */
+ * lists (precision 0 or 2; default 0 = never: the L1 it takes is worth more to a global-memory LU). */
 SGB_API int32_t gpu_kin_coop_set_smem_budget(uint32_t precision, uint32_t bytes);
 /* Clock cycles per phase of the cooperative kernel (rhs, Jacobian, factor, solves, -, whole
  * attempts), summed over CTAs' thread 0, in a build with -DSGB_COOP_PROFILE (zeros otherwise);

@@ -77,7 +77,10 @@ __device__ unsigned long long g_coop_phase_cycles[8];
 // Shared-memory doubles before the mixed path's FP32 arrays.
 __host__ __device__ inline uint32_t coop_smem_doubles(uint32_t n, uint32_t R) { return 11u * n + 2u * R + 8u; }
 
-constexpr uint32_t kCoopSmemBudget = 200 * 1024;   // default: the term lists join shared memory while the total stays below this
+// Default budget up to which the term lists join shared memory: none. Measured on the 200-species
+// FP64 case, staging them (149 KB of shared memory per CTA) made the step 1.31x slower, because the
+// smaller L1 then caches less of the global-memory LU; callers may enable it per precision.
+constexpr uint32_t kCoopSmemBudget = 0;
 
 // Shared memory of one CTA: doubles, x32 (256 floats), pattern (n x 8 words), lcnt (n u16,
 // padded), then the LU (mixed always, n x ld floats; FP64 when it fits kCoopSmemLuF64Max), then
