@@ -648,6 +648,17 @@ struct CoopModule {
 CoopModule cm;
 constexpr uint32_t kCoopMaxCtasPerSm = 2;   // scratch slots per SM
 
+// Dynamic shared memory of a launch, and the L1 / shared split: when the LU lives in global memory
+// (FP64, large mechanisms: one CTA per SM) as much L1 as the launch's shared memory leaves, since the
+// elimination leans on L1; otherwise the driver's default split (several CTAs per SM).
+cudaError_t set_coop_attributes(void (*fn)(DevArgs, double *, uint64_t), int prec, const CoopMech &h, uint32_t budget) {
+    const CoopSmemLayout lay = coop_layout(prec, h, budget);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
+    if (e == cudaSuccess)
+        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, lay.lu_bytes ? -1 : 0);
+    return e;
+}
+
 size_t coop_smem_bytes(int prec, const CoopMech &h, uint32_t budget = kCoopSmemBudget) {
     return coop_layout(prec, h, budget).total;
 }
@@ -671,10 +682,8 @@ cudaError_t coop_launch(int prec, const DevArgs &A0, const CoopMech &head, doubl
     DevArgs A = A0;
     if (!A.coop_smem_budget) A.coop_smem_budget = kCoopSmemBudget;
     const size_t smem = coop_smem_bytes(prec, head, A.coop_smem_budget);
-    if (smem > 48 * 1024) {
-        cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-    }
+    cudaError_t ce = set_coop_attributes(fn, prec, head, A.coop_smem_budget);
+    if (ce != cudaSuccess) return ce;
     fn<<<grid, block, smem, s>>>(A, scratch, coop_scratch_doubles(prec, head));
     return cudaGetLastError();
 }
@@ -778,7 +787,7 @@ SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *L, float *kernel_ms) {
     void (*fn)(DevArgs, double *, uint64_t) = prec == 0 ? kin_coop_kernel<0> : kin_coop_kernel<2>;
     A.coop_smem_budget = cm.smem_budget[prec];
     const size_t smem = coop_smem_bytes(prec, cm.head, A.coop_smem_budget);
-    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    e = set_coop_attributes(fn, prec, cm.head, A.coop_smem_budget);
     if (e != cudaSuccess) return (int32_t)e;
     int fit = 0;
     e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&fit, fn, (int)cm.block[prec], smem);
