@@ -55,6 +55,13 @@ def _sources_newer(target: str, deps: list[str]) -> bool:
 
 def build(force: bool = False, jobs: int | None = None) -> str:
     os.makedirs(GEN, exist_ok=True)
+    # objects built with other flags (SGB_DEFINES variants) are rebuilt
+    stamp = os.path.join(BUILD, "flags.txt")
+    flags = " ".join(NV_FLAGS + CXX_FLAGS)
+    if not os.path.exists(stamp) or open(stamp).read() != flags:
+        force = True
+        with open(stamp, "w") as f:
+            f.write(flags)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".h", ".cuh"))]
     headers.append(os.path.join(ROOT, "include", "simstack_gpu.h"))
     # 1. generator
