@@ -648,15 +648,10 @@ struct CoopModule {
 CoopModule cm;
 constexpr uint32_t kCoopMaxCtasPerSm = 2;   // scratch slots per SM
 
-// Dynamic shared memory of a launch, and the L1 / shared split: when the LU lives in global memory
-// (FP64, large mechanisms: one CTA per SM) as much L1 as the launch's shared memory leaves, since the
-// elimination leans on L1; otherwise the driver's default split (several CTAs per SM).
+// Dynamic shared memory of a launch (the L1 / shared split is left to the driver: preferring L1
+// measured no faster for the global-memory FP64 LU at one CTA per SM, and cost occupancy at two).
 cudaError_t set_coop_attributes(void (*fn)(DevArgs, double *, uint64_t), int prec, const CoopMech &h, uint32_t budget) {
-    const CoopSmemLayout lay = coop_layout(prec, h, budget);
-    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)lay.total);
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, lay.lu_bytes ? -1 : 0);
-    return e;
+    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)coop_layout(prec, h, budget).total);
 }
 
 size_t coop_smem_bytes(int prec, const CoopMech &h, uint32_t budget = kCoopSmemBudget) {
