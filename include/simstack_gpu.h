@@ -286,8 +286,8 @@ SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *launch, float *kernel_m
 /* out[8]: n, R, LU non-zeros, Jacobian entries, L entries, U entries, LU updates, image bytes. */
 SGB_API int32_t gpu_kin_coop_info(uint64_t *out);
 /* Launch shape of the cooperative kernels per precision (0 or 2): threads per CTA (64..512,
- * multiple of 32) and resident CTAs per SM (1..2; capped by occupancy). Defaults: 512 x 1 for
- * both (measured fastest for FP64 on 200 species; the mixed FP32 LU fills one SM's shared memory). */
+ * multiple of 32) and resident CTAs per SM (1..2; capped by occupancy). Defaults: FP64 256 x 2
+ * (measured fastest on 200 species), mixed 512 x 1 (its FP32 LU fills one SM's shared memory). */
 SGB_API int32_t gpu_kin_coop_set_shape(uint32_t precision, uint32_t block, uint32_t ctas_per_sm);
 /* Shared-memory bytes per CTA up to which the cooperative kernel also stages the RHS / Jacobian term
  * lists (precision 0 or 2; default 0 = never: the L1 it takes is worth more to a global-memory LU). */

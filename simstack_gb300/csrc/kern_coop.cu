@@ -111,6 +111,7 @@ struct CoopCell {
     double *y, *ytmp, *fcn, *src, *qv, *rb, *xv, *K, *kr, *rate, *red;
     float *x32;
     Cf *a;          // dense LU [n][ld]
+    bool lu_global;         // the LU lives in global scratch (FP64, large mechanisms)
     const uint32_t *pat;    // shared: filled pattern, 8 words per row
     const uint16_t *lcnt;   // shared: rows below the diagonal per column
     double *js;     // mixed: Jacobian entries (a = -J) in FP64
@@ -311,14 +312,36 @@ struct CoopCell {
                     live |= 1u << c;
                 }
             }
-            for (uint32_t i = k + 1 + warp; i < n; i += W) {
-                if (!bit(i, k)) continue;   // same for the whole warp
-                Cf *row = a + (size_t)i * ld;
-                const Cf l = row[k];
+            if (lu_global) {
+                // global-memory LU: the row's elements first, then the updates, so the loads issue
+                // back to back instead of each waiting behind the previous element's store
+                for (uint32_t i = k + 1 + warp; i < n; i += W) {
+                    if (!bit(i, k)) continue;   // same for the whole warp
+                    Cf *row = a + (size_t)i * ld;
+                    const Cf l = row[k];
+                    Cf v[kCoopMaxCols];
 #pragma unroll
-                for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
-                    const uint32_t j = k + 1 + lane + 32u * c;
-                    if ((live >> c) & 1u) row[j] = sgb_fma(-l, pv[c], row[j]);
+                    for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
+                        const uint32_t j = k + 1 + lane + 32u * c;
+                        v[c] = (Cf)0.0;
+                        if ((live >> c) & 1u) v[c] = row[j];
+                    }
+#pragma unroll
+                    for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
+                        const uint32_t j = k + 1 + lane + 32u * c;
+                        if ((live >> c) & 1u) row[j] = sgb_fma(-l, pv[c], v[c]);
+                    }
+                }
+            } else {
+                for (uint32_t i = k + 1 + warp; i < n; i += W) {
+                    if (!bit(i, k)) continue;
+                    Cf *row = a + (size_t)i * ld;
+                    const Cf l = row[k];
+#pragma unroll
+                    for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
+                        const uint32_t j = k + 1 + lane + 32u * c;
+                        if ((live >> c) & 1u) row[j] = sgb_fma(-l, pv[c], row[j]);
+                    }
                 }
             }
             sync();
@@ -580,6 +603,7 @@ __global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant_
         C.a = lay.lu_bytes ? (typename CoopCell<PREC>::Cf *)(smb + lay.lu) : (typename CoopCell<PREC>::Cf *)g;
         C.js = nullptr;
     }
+    C.lu_global = PREC == 0 && lay.lu_bytes == 0;
     if (lay.terms_bytes) {   // the RHS / Jacobian term lists, once per CTA
         const CoopMech *h = C.tb.h;
         const uint4 *src = (const uint4 *)((const unsigned char *)A.tables + h->off_reac);
@@ -640,8 +664,8 @@ struct CoopModule {
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
     uint32_t ir_sweeps = 1;
     float last_ms = 0.0f;
-    uint32_t block[3] = {512, 0, 512};    // threads per CTA by precision (0 FP64, 2 mixed)
-    uint32_t ctas[3] = {1, 0, 1};         // resident CTAs per SM by precision
+    uint32_t block[3] = {256, 0, 512};    // threads per CTA by precision (0 FP64, 2 mixed)
+    uint32_t ctas[3] = {2, 0, 1};         // resident CTAs per SM by precision
     uint32_t smem_budget[3] = {kCoopSmemBudget, 0, kCoopSmemBudget};
     int sms = 0;
 };
