@@ -111,7 +111,7 @@ struct CoopCell {
     double *y, *ytmp, *fcn, *src, *qv, *rb, *xv, *K, *kr, *rate, *red;
     float *x32;
     Cf *a;          // dense LU [n][ld]
-    bool lu_global;         // the LU lives in global scratch (FP64, large mechanisms)
+    bool lu_global;         // eliminate with loads before stores (the LU lives in global scratch: FP64, large)
     const uint32_t *pat;    // shared: filled pattern, 8 words per row
     const uint16_t *lcnt;   // shared: rows below the diagonal per column
     double *js;     // mixed: Jacobian entries (a = -J) in FP64
@@ -603,7 +603,10 @@ __global__ void __launch_bounds__(512, 1) kin_coop_kernel(const __grid_constant_
         C.a = lay.lu_bytes ? (typename CoopCell<PREC>::Cf *)(smb + lay.lu) : (typename CoopCell<PREC>::Cf *)g;
         C.js = nullptr;
     }
-    C.lu_global = PREC == 0 && lay.lu_bytes == 0;
+#ifndef SGB_COOP_LOADS_FIRST_SMEM
+#define SGB_COOP_LOADS_FIRST_SMEM 0
+#endif
+    C.lu_global = (PREC == 0 && lay.lu_bytes == 0) || (SGB_COOP_LOADS_FIRST_SMEM && n >= 64);
     if (lay.terms_bytes) {   // the RHS / Jacobian term lists, once per CTA
         const CoopMech *h = C.tb.h;
         const uint4 *src = (const uint4 *)((const unsigned char *)A.tables + h->off_reac);
