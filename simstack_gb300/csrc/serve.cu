@@ -12,14 +12,16 @@
 // once -- 16 bytes of HBM traffic per cell and species per coupling step.
 //
 // Coupling step (operator split, chemistry first, as dbd_scene.cpp:263-265):
-// [cursor reset] -> [chemistry: persistent queue kernel over the request's
-// zone block, 1 s] -> [advection]. Captured once per request into a CUDA graph
-// and replayed every step on the request's own stream; each request has its
-// own queue scratch, so requests run side by side.
+// [cursor reset] -> [chemistry over the request's zone block, 1 s: the
+// persistent queue kernel for the shipped or a KinMech table mechanism, the
+// cooperative one-CTA-per-cell kernel for a large mechanism] -> [advection].
+// Captured once per request into a CUDA graph and replayed every step on the
+// request's own stream; each request has its own queue scratch, so requests
+// run side by side.
 //
 // Serving: requests are admitted first-in first-out while their device
-// footprint (zone block + queue scratch + tables) fits the HBM budget and the
-// device's free memory; their state stays device-resident across coupling
+// footprint (zone block + queue scratch + tables) fits the HBM budget (set at
+// open from the device's free memory); their state stays device-resident across coupling
 // steps; the host drives the engine with gpu_serve_progress(), which retires
 // finished requests (result copied to host, memory freed), admits waiting
 // ones, and launches the next coupling step of every running request whose
