@@ -150,6 +150,7 @@ def lib() -> C.CDLL:
             "gpu_kin_wait": (i32, [C.POINTER(f), C.POINTER(f)]),
             "gpu_kin_set_mode": (i32, [u32]),
             "gpu_kin_advance_queue": (i32, [C.POINTER(GpuKinLaunch), C.POINTER(f)]),
+            "gpu_kin_advance_pipelined": (i32, [C.POINTER(GpuKinLaunch), vp, vp, u64, u64, u32, C.POINTER(f)]),
             "gpu_kin_set_tuning": (i32, [C.POINTER(GpuKinTuning)]),
             "gpu_kin_get_tuning": (i32, [u32, C.POINTER(GpuKinTuning)]),
             "gpu_kin_autotune": (i32, [C.POINTER(GpuKinLaunch), u32, C.POINTER(GpuKinTuning)]),
@@ -534,6 +535,17 @@ class Module:
         c = C.c_uint32()
         check(lib().gpu_kin_parked_cells(C.byref(c)), "gpu_kin_parked_cells")
         return c.value
+
+    def integrate_pipelined(self, z: ZoneBlock, duration: float, precision: int = 0, chunks: int = 4,
+                            device_base: int | None = None) -> float:
+        """Host block in, results back, with the copies overlapped with the kernels
+        (gpu_kin_advance_pipelined); the host block should be page-locked. Returns device ms."""
+        base = device_base if device_base is not None else self.alloc(z.nbytes)
+        ms = C.c_float()
+        L = z.launch(base, precision, duration, z.cells)
+        check(lib().gpu_kin_advance_pipelined(C.byref(L), _p(z.data), base, z.rows, z.mutable_rows, chunks, C.byref(ms)),
+              "gpu_kin_advance_pipelined")
+        return ms.value
 
     # cooperative kernels (one CTA per cell): mechanisms beyond the KinMech tables
     def coop_set_mech(self, model: "Model", meth: KinMethod | None = None, ctl: KinControl | None = None) -> None:

@@ -77,6 +77,11 @@ struct Module {
     float last_ms = 0.0f;
     // straggler hand-off: cells past `straggler_budget` step attempts in one launch are parked
     // and finished by the cooperative kernel (one CTA per cell) on the same stream
+    cudaStream_t copy_in = nullptr, copy_out = nullptr;   // pipelined advance: upload and download streams
+    cudaStream_t kern2 = nullptr;                         // ... and a second kernel stream
+    static constexpr int kMaxChunks = 16;
+    cudaEvent_t ev_in[kMaxChunks] = {}, ev_kern[kMaxChunks] = {};
+    cudaEvent_t pipe_begin = nullptr, pipe_end = nullptr, pipe_after = nullptr;
     uint32_t straggler_budget = 600;  // FP64 step attempts per launch before a cell is handed on
     uint32_t straggler_block = 128;   // threads per parked cell
     SuspendRec *d_suspend = nullptr;
@@ -137,7 +142,7 @@ cudaError_t occupancy(uint32_t prec, const GpuKinTuning &t, int *blocks) {
     return occupancy_table_p2(t.kind, t.block, kTableBytes, blocks);
 }
 
-cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A);
+cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A, cudaStream_t stream = nullptr);
 
 // Local memory per thread the kernel of (precision, tuning) needs.
 cudaError_t local_bytes(uint32_t prec, const GpuKinTuning &t, size_t *bytes) {
@@ -178,9 +183,11 @@ cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &
     return coop_launch(0, R, g.coop_head, g.d_coop_scratch, g.coop_grid, g.straggler_block, g.stream);
 }
 
-// The lane kernels (one cell per thread) for `A`.
-cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A) {
+// The lane kernels (one cell per thread) for `A`, on `stream` (default: the module stream); the
+// queue kernels take their cells from A.cursor.
+cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A, cudaStream_t stream) {
     if (A.lanes == 0) return cudaSuccess;
+    if (!stream) stream = g.stream;
     Shape s;
     s.kind = t.kind;
     s.block = t.block;
@@ -197,23 +204,23 @@ cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A)
         uint32_t resident = (uint32_t)per_sm * (uint32_t)g.sms;
         uint32_t needed = (A.lanes + t.block - 1) / t.block;
         s.grid = resident < needed ? resident : needed;
-        e = cudaMemsetAsync(g.d_cursor, 0, sizeof(uint32_t), g.stream);
+        e = cudaMemsetAsync(A.cursor, 0, sizeof(uint32_t), stream);
         if (e != cudaSuccess) return e;
     }
     if (prec == 2 && g.mixed_variant == 1) {
-        if (g.generated) return launch_air_p3(s, A, g.stream);
+        if (g.generated) return launch_air_p3(s, A, stream);
         s.variant = 0;
-        return launch_table_p3(s, A, g.stream);
+        return launch_table_p3(s, A, stream);
     }
     if (g.generated) {
-        if (prec == 0) return launch_air_p0(s, A, g.stream);
-        if (prec == 1) return launch_air_p1(s, A, g.stream);
-        return launch_air_p2(s, A, g.stream);
+        if (prec == 0) return launch_air_p0(s, A, stream);
+        if (prec == 1) return launch_air_p1(s, A, stream);
+        return launch_air_p2(s, A, stream);
     }
     s.variant = 0;
-    if (prec == 0) return launch_table_p0(s, A, g.stream);
-    if (prec == 1) return launch_table_p1(s, A, g.stream);
-    return launch_table_p2(s, A, g.stream);
+    if (prec == 0) return launch_table_p0(s, A, stream);
+    if (prec == 1) return launch_table_p1(s, A, stream);
+    return launch_table_p2(s, A, stream);
 }
 
 cudaError_t check_launch(const GpuKinLaunch *L) {
@@ -304,10 +311,12 @@ SGB_API int32_t gpu_init(uint32_t device_index, uint64_t arena_bytes, GpuInfo *i
     info->arena_bytes = arena_bytes;
     e = cudaMalloc(&g.d_tables, kTableBytes);
     if (e != cudaSuccess) return (int32_t)e;
-    e = cudaMalloc((void **)&g.d_cursor, 256);   // cursor at +0, error flag at +128
+    // cursor at +0, error flag at +128, the pipelined advance's per-chunk cursors from +256 (128 B apart)
+    const size_t cursor_bytes = 256 + (size_t)Module::kMaxChunks * 128;
+    e = cudaMalloc((void **)&g.d_cursor, cursor_bytes);
     if (e != cudaSuccess) return (int32_t)e;
     g.d_error = (uint32_t *)((uint8_t *)g.d_cursor + 128);
-    cudaMemset(g.d_cursor, 0, 256);
+    cudaMemset(g.d_cursor, 0, cursor_bytes);
     if (!g.d_suspend) {
         e = cudaMalloc((void **)&g.d_suspend, (size_t)kSuspendCap * sizeof(SuspendRec) + 256);
         if (e != cudaSuccess) return (int32_t)e;
@@ -465,6 +474,80 @@ SGB_API int32_t gpu_kin_advance_async(const GpuKinLaunch *launch, void *host_blo
     e = cudaMemcpy2DAsync(host_block, pitch, device_block, pitch, width, mutable_rows, cudaMemcpyDeviceToHost, g.stream);
     if (e != cudaSuccess) return (int32_t)e;
     cudaEventRecord(g.async_end, g.stream);
+    return (int32_t)cudaGetLastError();
+}
+
+// The same work as gpu_kin_advance_async + gpu_kin_wait, with lanes [0, lane_count) split into
+// `chunks` column ranges whose uploads, kernels and downloads overlap: chunk c+1 uploads on one
+// stream while chunk c integrates and chunk c-1 downloads on another. Each chunk's kernel is a
+// full advance of its lanes (same results per cell). Chunk kernels alternate between two kernel
+// streams, each queue kernel with its own cursor, so chunk c+1's CTAs take the SMs that chunk
+// c's last cells leave idle; the kernels never wait on one another. With the FP64 straggler
+// hand-off on (it shares one suspension list) the chunk kernels run in order on the module
+// stream. Waits; total_ms is the time on the device from the first upload to the last download.
+SGB_API int32_t gpu_kin_advance_pipelined(const GpuKinLaunch *launch, void *host_block, void *device_block, uint64_t rows,
+                                          uint64_t mutable_rows, uint32_t chunks, float *total_ms) {
+    cudaError_t e = check_launch(launch);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (!host_block || !device_block || mutable_rows > rows || chunks == 0 || chunks > (uint32_t)Module::kMaxChunks)
+        return (int32_t)cudaErrorInvalidValue;
+    if (!g.copy_in) {
+        e = cudaStreamCreateWithFlags(&g.copy_in, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g.copy_out, cudaStreamNonBlocking);
+        for (int c = 0; c < Module::kMaxChunks && e == cudaSuccess; ++c) {
+            e = cudaEventCreateWithFlags(&g.ev_in[c], cudaEventDisableTiming);
+            if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g.ev_kern[c], cudaEventDisableTiming);
+        }
+        if (e == cudaSuccess) e = cudaEventCreate(&g.pipe_begin);
+        if (e == cudaSuccess) e = cudaEventCreate(&g.pipe_end);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&g.pipe_after, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&g.kern2, cudaStreamNonBlocking);
+        if (e != cudaSuccess) return (int32_t)e;
+    }
+    const bool serial = g.straggler_budget && g.d_coop_image && launch->precision == 0;
+    const uint64_t P = launch->padded, lanes = launch->lane_count ? launch->lane_count : launch->padded;
+    const uint64_t pitch = P * sizeof(double);
+    const uint64_t per = (lanes + chunks - 1) / chunks;
+    uint8_t *hb = (uint8_t *)host_block, *db = (uint8_t *)device_block;
+    // everything already queued on the module stream (an earlier async advance) comes first
+    e = cudaEventRecord(g.pipe_after, g.stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(g.copy_in, g.pipe_after, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(g.kern2, g.pipe_after, 0);
+    if (e == cudaSuccess) e = cudaEventRecord(g.pipe_begin, g.copy_in);
+    for (uint32_t c = 0; c < chunks && e == cudaSuccess; ++c) {
+        const uint64_t first = (uint64_t)c * per, count = first < lanes ? (lanes - first < per ? lanes - first : per) : 0;
+        if (count == 0) break;
+        cudaStream_t ks = serial || (c & 1) == 0 ? g.stream : g.kern2;
+        e = cudaMemcpy2DAsync(db + first * 8, pitch, hb + first * 8, pitch, count * 8, rows, cudaMemcpyHostToDevice, g.copy_in);
+        if (e == cudaSuccess) e = cudaEventRecord(g.ev_in[c], g.copy_in);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ks, g.ev_in[c], 0);
+        if (e != cudaSuccess) break;
+        GpuKinLaunch Lc = *launch;   // the chunk: every row pointer moved to its first lane
+        double **rowp[12] = {&Lc.y, &Lc.h, &Lc.steps, &Lc.rejects, &Lc.pulses, &Lc.failed,
+                             &Lc.k, &Lc.src, &Lc.pulse, &Lc.period, &Lc.pulse_first, &Lc.pulse_count};
+        for (double **r : rowp) *r += first;
+        Lc.lane_count = (uint32_t)count;
+        DevArgs A;
+        fill_args(&Lc, &A);
+        if (serial) {
+            e = launch_advance(launch->precision, g.tuning[launch->precision], A);
+        } else {
+            A.cursor = (uint32_t *)((uint8_t *)g.d_cursor + 256 + (size_t)c * 128);
+            e = launch_lanes(launch->precision, g.tuning[launch->precision], A, ks);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(g.ev_kern[c], ks);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(g.copy_out, g.ev_kern[c], 0);
+        if (e == cudaSuccess)
+            e = cudaMemcpy2DAsync(hb + first * 8, pitch, db + first * 8, pitch, count * 8, mutable_rows, cudaMemcpyDeviceToHost,
+                                  g.copy_out);
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(g.pipe_end, g.copy_out);
+    if (e == cudaSuccess) e = cudaEventSynchronize(g.pipe_end);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (total_ms) cudaEventElapsedTime(total_ms, g.pipe_begin, g.pipe_end);
+    ++g.launches;
+    e = read_error_flag();
+    if (e != cudaSuccess) return (int32_t)e;
     return (int32_t)cudaGetLastError();
 }
 
