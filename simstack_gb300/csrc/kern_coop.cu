@@ -74,6 +74,15 @@ __device__ unsigned long long g_coop_phase_cycles[8];
 #define SGB_PHASE(i, stmt) stmt
 #endif
 
+// Pivots per elimination pass of the FP64 factorisation with its LU in global memory (1, 2 or 4;
+// the same bits for any). Measured on 200 species / 1,200 reactions, 1,216 cells x 2 s, 256
+// threads x 2 CTAs per SM: 1 -> 6,817 ms, 2 -> 5,805 ms, 4 -> 6,272 ms (the one-warp panel grows).
+// The shared-memory LUs (FP64 of small mechanisms, the mixed path's FP32) stay pivot by pivot:
+// the mixed kernel measured 2,392 ms pivot by pivot against 2,745 (2) and 2,630 (4).
+#ifndef SGB_COOP_PIVOT_BLOCK
+#define SGB_COOP_PIVOT_BLOCK 2
+#endif
+
 // Shared-memory doubles before the mixed path's FP32 arrays.
 __host__ __device__ inline uint32_t coop_smem_doubles(uint32_t n, uint32_t R) { return 11u * n + 2u * R + 8u; }
 
@@ -268,6 +277,12 @@ struct CoopCell {
     // columns are walked densely; the pattern bits select the elements the
     // reference updates.
     __device__ void factor(Cf ghinv) {
+#if SGB_COOP_PIVOT_BLOCK > 1
+        if (!kMixed && lu_global) {
+            factor_block<SGB_COOP_PIVOT_BLOCK>(ghinv);
+            return;
+        }
+#endif
         for (uint32_t k = 0; k < n; ++k) {
             const uint32_t nl = lcnt[k];
             Cf inv;
@@ -343,6 +358,113 @@ struct CoopCell {
                         if ((live >> c) & 1u) row[j] = sgb_fma(-l, pv[c], row[j]);
                     }
                 }
+            }
+            sync();
+        }
+        sync();
+    }
+
+    // B pivots per pass (k .. k+B-1). Panel: warp 0 gives each row r of the block the updates of
+    // the block's pivots before it, in order, then takes 1/U(r,r), and stages row r's U part in
+    // shared memory. Trailing rows i >= k+B, one warp per row: the row's block entries become its
+    // multipliers in order (a[i][k+p] takes the updates of pivots k+q, q < p, then the scaling by
+    // 1/U(k+p,k+p)), and each a[i][j], j >= k+B, takes the block's pivots' updates in ascending
+    // order, loaded once and stored once. Every element receives the operations of the pivot-by-
+    // pivot order, in that order, with 1/B of the passes over the trailing rows (the LU of a large
+    // mechanism lives in L2) and of the barriers. The staged rows use the stage vectors K (free
+    // until the stages begin) and the inverses red[4..7], so B <= 4.
+    template <uint32_t B>
+    __device__ void factor_block(Cf ghinv) {
+        static_assert(B >= 1 && B <= 4 && 32 % B == 0, "block of 1, 2 or 4 pivots");
+        static_assert(kCoopMaxCols * B <= 32, "column masks in one word");
+        Cf *inv_s = (Cf *)(red + 4);
+        Cf *u = (Cf *)K;   // [B][n] staged pivot rows, zero off the pattern
+        for (uint32_t k = 0; k < n; k += B) {
+            const uint32_t nb = n - k < B ? n - k : B;
+            if (warp == 0) {   // the panel
+                for (uint32_t r = k; r < k + nb; ++r) {
+                    Cf *rr = a + (size_t)r * ld;
+                    for (uint32_t q = k; q < r; ++q) {
+                        if (!bit(r, q)) continue;   // same for the whole warp
+                        const Cf l = rr[q] * inv_s[q - k];
+                        const Cf *uq = u + (size_t)(q - k) * n;
+                        for (uint32_t j = q + 1 + lane; j < n; j += 32)
+                            if (bit(q, j)) rr[j] = sgb_fma(-l, uq[j], rr[j]);
+                        __syncwarp();
+                        if (lane == 0) rr[q] = l;
+                        __syncwarp();
+                    }
+                    if (lane == 0) {
+                        const Cf v = (Cf)1.0 / (rr[r] + ghinv);
+                        rr[r] = v;
+                        inv_s[r - k] = v;
+                    }
+                    __syncwarp();
+                    Cf *ur = u + (size_t)(r - k) * n;
+                    for (uint32_t j = r + 1 + lane; j < n; j += 32) ur[j] = bit(r, j) ? rr[j] : (Cf)0.0;
+                    __syncwarp();
+                }
+            }
+            sync();
+            const uint32_t j0 = k + nb;
+            if (j0 >= n) break;
+            const uint32_t bmask = (1u << nb) - 1u;
+            // per lane: which block pivots update column j0 + lane + 32c (bits c*B + p)
+            uint32_t live = 0;
+#pragma unroll
+            for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
+                const uint32_t j = j0 + lane + 32u * c;
+                if (j >= n) continue;
+#pragma unroll
+                for (uint32_t p = 0; p < B; ++p)
+                    if (p < nb && bit(k + p, j)) live |= 1u << (c * B + p);
+            }
+            // inner[p]: block pivots q < p whose row has column k+p
+            uint32_t inner = 0;
+#pragma unroll
+            for (uint32_t p = 1; p < B; ++p)
+#pragma unroll
+                for (uint32_t q = 0; q < p; ++q)
+                    if (p < nb && bit(k + q, k + p)) inner |= 1u << (p * B + q);
+            for (uint32_t i = j0 + warp; i < n; i += W) {
+                // row i's pattern bits at the block's columns (k is a multiple of B: one word)
+                const uint32_t bm = (pat[i * 8u + (k >> 5)] >> (k & 31u)) & bmask;
+                if (!bm) continue;   // same for the whole warp
+                Cf *row = a + (size_t)i * ld;
+                Cf l[B];
+#pragma unroll
+                for (uint32_t p = 0; p < B; ++p) {
+                    l[p] = (Cf)0.0;
+                    if ((bm >> p) & 1u) {
+                        Cf x = row[k + p];
+#pragma unroll
+                        for (uint32_t q = 0; q < p; ++q)
+                            if (((bm >> q) & 1u) && ((inner >> (p * B + q)) & 1u)) x = sgb_fma(-l[q], u[(size_t)q * n + k + p], x);
+                        l[p] = x * inv_s[p];
+                    }
+                }
+                Cf v[kCoopMaxCols];
+#pragma unroll
+                for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
+                    const uint32_t j = j0 + lane + 32u * c;
+                    v[c] = (Cf)0.0;
+                    if ((live >> (c * B)) & bm) v[c] = row[j];
+                }
+#pragma unroll
+                for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
+                    const uint32_t j = j0 + lane + 32u * c;
+                    const uint32_t m = (live >> (c * B)) & bm;
+                    if (!m) continue;
+                    Cf x = v[c];
+#pragma unroll
+                    for (uint32_t p = 0; p < B; ++p)
+                        if ((m >> p) & 1u) x = sgb_fma(-l[p], u[(size_t)p * n + j], x);
+                    row[j] = x;
+                }
+                __syncwarp();   // every lane has read the block entries
+#pragma unroll
+                for (uint32_t p = 0; p < B; ++p)
+                    if (lane == p && ((bm >> p) & 1u)) row[k + p] = l[p];
             }
             sync();
         }
