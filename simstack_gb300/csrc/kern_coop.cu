@@ -275,7 +275,9 @@ struct CoopCell {
     // In place: a -> L\U of (I ghinv - J), diagonal holding 1/U(k,k); pivot by
     // pivot (kin_solver.h:97-113 applies the same updates row by row). Rows and
     // columns are walked densely; the pattern bits select the elements the
-    // reference updates.
+    // reference updates. The warp that updates row i also forms its multiplier
+    // l(i,k) = a[i][k] * (1/U(k,k)) and stores it once the row is done, so a pivot
+    // needs one barrier (FP32) or two (FP64: the shared inverse).
     __device__ void factor(Cf ghinv) {
 #if SGB_COOP_PIVOT_BLOCK > 1
         if (!kMixed && lu_global) {
@@ -288,7 +290,7 @@ struct CoopCell {
             Cf inv;
             if constexpr (kMixed) {
                 // FP32: every thread divides (cheap on the FP32 pipe); the inverted diagonal is
-                // stored after the barrier below, once every thread has read a[k][k]
+                // stored after the pivot's closing barrier, once every thread has read a[k][k]
                 if (nl == 0) {   // nothing below the pivot: the next pivot reads none of this pivot's writes
                     if (tid == 0) a[(size_t)k * ld + k] = (Cf)1.0 / (a[(size_t)k * ld + k] + ghinv);
                     continue;
@@ -305,13 +307,6 @@ struct CoopCell {
                 if (nl == 0) continue;
                 sync();
                 inv = *inv_s;
-            }
-            // L column k: l_i = a[i][k] / U(k,k)
-            for (uint32_t i = k + 1 + tid; i < n; i += NT)
-                if (bit(i, k)) a[(size_t)i * ld + k] = a[(size_t)i * ld + k] * inv;
-            sync();
-            if constexpr (kMixed) {
-                if (tid == 0) a[(size_t)k * ld + k] = inv;
             }
             // pivot row k (final) cached per lane: columns k+1+lane+32c in the pattern
             const uint32_t width = n - 1 - k, chunks = (width + 31) / 32;
@@ -333,7 +328,7 @@ struct CoopCell {
                 for (uint32_t i = k + 1 + warp; i < n; i += W) {
                     if (!bit(i, k)) continue;   // same for the whole warp
                     Cf *row = a + (size_t)i * ld;
-                    const Cf l = row[k];
+                    const Cf l = row[k] * inv;
                     Cf v[kCoopMaxCols];
 #pragma unroll
                     for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
@@ -346,20 +341,27 @@ struct CoopCell {
                         const uint32_t j = k + 1 + lane + 32u * c;
                         if ((live >> c) & 1u) row[j] = sgb_fma(-l, pv[c], v[c]);
                     }
+                    __syncwarp();   // every lane has read a[i][k]
+                    if (lane == 0) row[k] = l;
                 }
             } else {
                 for (uint32_t i = k + 1 + warp; i < n; i += W) {
                     if (!bit(i, k)) continue;
                     Cf *row = a + (size_t)i * ld;
-                    const Cf l = row[k];
+                    const Cf l = row[k] * inv;
 #pragma unroll
                     for (uint32_t c = 0; c < kCoopMaxCols; ++c) {
                         const uint32_t j = k + 1 + lane + 32u * c;
                         if ((live >> c) & 1u) row[j] = sgb_fma(-l, pv[c], row[j]);
                     }
+                    __syncwarp();
+                    if (lane == 0) row[k] = l;
                 }
             }
             sync();
+            if constexpr (kMixed) {   // every thread has read a[k][k]
+                if (tid == 0) a[(size_t)k * ld + k] = inv;
+            }
         }
         sync();
     }
