@@ -199,7 +199,7 @@ def flops_per_step(model) -> dict:
 # Nearly all of it is local-memory spill traffic, which grows with the cell-steps a launch executes;
 # the bench scales it to its own launch.
 DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 2045.3}
-PIPELINE_CHUNKS = (2, 4, 8, 16)   # lane-chunk counts tried for the pipelined end-to-end call
+PIPELINE_CHUNKS = (2, 4)   # lane-chunk counts tried for the pipelined end-to-end call (8 and 16 measured slower)
 
 
 def hbm_bytes_per_cell(n: int, R: int) -> int:
