@@ -473,6 +473,18 @@ struct CoopCell {
         sync();
     }
 
+    // Row elements [k0, min(k0 + kSolveBatch, end)) of a block's pattern columns, loaded together
+    // ahead of the FMA chain that uses them (the LU of a large mechanism lives in L2).
+    static constexpr uint32_t kSolveBatch = 8;
+    __device__ __forceinline__ static void load_batch(Cf (&r)[kSolveBatch], const Cf *row, uint32_t k0, uint32_t end,
+                                                      uint32_t w) {
+#pragma unroll
+        for (uint32_t q = 0; q < kSolveBatch; ++q) {
+            r[q] = (Cf)0.0;
+            if (k0 + q < end && ((w >> (k0 + q)) & 1u)) r[q] = row[k0 + q];
+        }
+    }
+
     // x = (LU)^-1 x in place, in 32-column blocks. Forward (unit L): a warp
     // solves the diagonal block with shuffles, then every row below takes the
     // block's updates in ascending column order. Backward (U, diagonal holding
@@ -480,6 +492,12 @@ struct CoopCell {
     // descending column order; a row's diagonal scaling follows its last update.
     template <class V>
     __device__ void solve(V *x) {
+        if constexpr (kMixed) solve_plain(x);   // FP32 LU in shared memory: element by element
+        else solve_batched(x);                  // FP64 LU, in L2 for large mechanisms: batched loads
+    }
+
+    template <class V>
+    __device__ void solve_plain(V *x) {
         const uint32_t nb = (n + 31) / 32;
         for (uint32_t b = 0; b < nb; ++b) {
             const uint32_t kb = b * 32;
@@ -534,6 +552,100 @@ struct CoopCell {
                 V xi = x[i];
                 for (uint32_t k = kend; k-- > kb;)
                     if ((w >> (k - kb)) & 1u) xi = sgb_fma(-(V)row[k], x[k], xi);
+                x[i] = xi;
+            }
+            sync();
+        }
+    }
+
+    // solve_plain's operations in its order, each row's pattern elements of a block loaded
+    // kSolveBatch at a time ahead of the FMAs that use them (measured on the 200-species FP64
+    // case: 1.05x the whole step; the mixed path's shared-memory LU measured 1.03x slower).
+    template <class V>
+    __device__ void solve_batched(V *x) {
+        const uint32_t nb = (n + 31) / 32;
+        for (uint32_t b = 0; b < nb; ++b) {
+            const uint32_t kb = b * 32;
+            const uint32_t kend = kb + 32 < n ? kb + 32 : n;
+            const uint32_t kn = kend - kb;   // columns in this block (32, or fewer in the last)
+            if (warp == 0) {
+                const uint32_t i = kb + lane;
+                V xi = i < n ? x[i] : (V)0.0;
+                const Cf *row = a + (size_t)(i < n ? i : 0) * ld + kb;
+                // this row's pattern bits for the block's columns, below the diagonal only
+                const uint32_t w = i < n ? pat[i * 8u + b] & ((1u << lane) - 1u) : 0u;
+                for (uint32_t k0 = 0; k0 < kn; k0 += kSolveBatch) {
+                    Cf r[kSolveBatch];
+                    load_batch(r, row, k0, kn, w);
+#pragma unroll
+                    for (uint32_t q = 0; q < kSolveBatch; ++q) {
+                        if (k0 + q >= kn) break;
+                        const V xk = __shfl_sync(0xffffffffu, xi, k0 + q);
+                        if ((w >> (k0 + q)) & 1u) xi = sgb_fma(-(V)r[q], xk, xi);
+                    }
+                }
+                if (i < n) x[i] = xi;
+            }
+            sync();
+            for (uint32_t i = kend + tid; i < n; i += NT) {
+                const Cf *row = a + (size_t)i * ld + kb;
+                const uint32_t w = pat[i * 8u + b];
+                if (!w) continue;
+                V xi = x[i];
+                for (uint32_t k0 = 0; k0 < kn; k0 += kSolveBatch) {
+                    Cf r[kSolveBatch];
+                    load_batch(r, row, k0, kn, w);
+#pragma unroll
+                    for (uint32_t q = 0; q < kSolveBatch; ++q)
+                        if (k0 + q < kn && ((w >> (k0 + q)) & 1u)) xi = sgb_fma(-(V)r[q], x[kb + k0 + q], xi);
+                }
+                x[i] = xi;
+            }
+            sync();
+        }
+        for (uint32_t b = nb; b-- > 0;) {
+            const uint32_t kb = b * 32;
+            const uint32_t kend = kb + 32 < n ? kb + 32 : n;
+            const uint32_t kn = kend - kb;
+            if (warp == 0) {
+                const uint32_t i = kb + lane;
+                V xi = i < n ? x[i] : (V)0.0;
+                const Cf *row = a + (size_t)(i < n ? i : 0) * ld + kb;
+                // this row's pattern bits for the block's columns, above the diagonal only (columns < n)
+                const uint32_t w = i < n ? pat[i * 8u + b] & ~((2u << lane) - 1u) : 0u;
+                const V d = i < n ? (V)row[lane] : (V)0.0;   // 1/U(i,i)
+                // batches from the block's last column down, each in descending order
+                for (uint32_t top = kn; top > 0;) {
+                    const uint32_t k0 = top > kSolveBatch ? top - kSolveBatch : 0;
+                    Cf r[kSolveBatch];
+                    load_batch(r, row, k0, top, w);
+#pragma unroll
+                    for (uint32_t q = kSolveBatch; q-- > 0;) {
+                        if (k0 + q >= top) continue;
+                        const uint32_t kk = k0 + q;
+                        if (lane == kk) xi = xi * d;   // row kb+kk: all its updates are in
+                        const V xk = __shfl_sync(0xffffffffu, xi, kk);
+                        if ((w >> kk) & 1u) xi = sgb_fma(-(V)r[q], xk, xi);
+                    }
+                    top = k0;
+                }
+                if (i < n) x[i] = xi;
+            }
+            sync();
+            for (uint32_t i = tid; i < kb; i += NT) {
+                const Cf *row = a + (size_t)i * ld + kb;
+                const uint32_t w = pat[i * 8u + b];
+                if (!w) continue;
+                V xi = x[i];
+                for (uint32_t top = kn; top > 0;) {
+                    const uint32_t k0 = top > kSolveBatch ? top - kSolveBatch : 0;
+                    Cf r[kSolveBatch];
+                    load_batch(r, row, k0, top, w);
+#pragma unroll
+                    for (uint32_t q = kSolveBatch; q-- > 0;)
+                        if (k0 + q < top && ((w >> (k0 + q)) & 1u)) xi = sgb_fma(-(V)r[q], x[kb + k0 + q], xi);
+                    top = k0;
+                }
                 x[i] = xi;
             }
             sync();
