@@ -41,6 +41,15 @@ MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
 HBM_FALLBACK_GBS = 6800.0
 
 
+WORKLOADS = {
+    "air-1048576x10s": "default, the headline: shipped mechanism, 1,048,576 cells x 10 s, mixed and FP64",
+    "air-4096x1s": "shipped mechanism, 4,096 cells x 1 s (the reference's CPU-runnable case)",
+    "uneven-262144x60s": "uneven stiffness: 262,144 cells x 60 s with a discharge source, static vs queue vs hand-off",
+    "mech200-65536x10s": "200-species / 1,200-reaction synthetic mechanism, 65,536 cells x 10 s, one CTA per cell",
+    "serve-poisson200": "served requests (Poisson arrivals at 200 req/s) with film advection, p50/p99 latency",
+}
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -53,18 +62,15 @@ def parse():
     ap.add_argument("--cpu-seconds", type=float, default=10.0, help="target length of the CPU-baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--seed", type=int, default=1)
-    ap.add_argument("--workload", choices=["config2", "config1", "config3", "config4", "config5"], default="config2",
-                    help="config2 (default, the headline): 1,048,576 cells x 10 s; config1: 4,096 cells x 1 s; "
-                         "config3: uneven stiffness, 262,144 cells x 60 s with a discharge source, static vs queue; "
-                         "config4: 200-species / 1,200-reaction synthetic mechanism, one CTA per cell; "
-                         "config5: served requests (Poisson arrivals) with film advection, p50/p99 latency")
-    ap.add_argument("--requests", type=int, default=48, help="config5: requests in the served sample")
+    ap.add_argument("--workload", choices=list(WORKLOADS), default="air-1048576x10s",
+                    help="; ".join(f"{k}: {v}" for k, v in WORKLOADS.items()))
+    ap.add_argument("--requests", type=int, default=48, help="serve-poisson200: requests in the served sample")
     ap.add_argument("--tuning", default=None,
                     help="--profile-case: launch shape block,variant,ctas_per_sm of the CTA-synchronous queue kernel")
     ap.add_argument("--mixed-variant", type=int, choices=[0, 1], default=None,
                     help="--profile-case mixed: 0 = FP64 state with refinement, 1 = double-float state (default)")
     ap.add_argument("--fp64-cells", type=int, default=1216,
-                    help="config4: cells of the FP64 comparison sample (the first cells of the workload)")
+                    help="mech200-65536x10s: cells of the FP64 comparison sample (the first cells of the workload)")
     ap.add_argument("--profile-case", choices=["f64", "mixed", "f32", "coop-f64", "coop-mixed"], default=None,
                     help="one advance of --cells x --duration at this precision, then exit (ncu captures): the "
                          "queue kernel on the shipped mechanism, or the cooperative kernel on the 200-species one")
@@ -551,24 +557,24 @@ def run_ours(args):
     grp.close()
 
 
-# Config 3: the shipped source model's per-second discharge source at a power
+# Uneven stiffness: the shipped source model's per-second discharge source at a power
 # drawn log-uniform over 3 decades from P0 (W/cm^3); P0 = 1e-2 gives accepted
 # steps from ~150 to ~2,700 per cell over 60 s on these initial states (p50 ~280),
 # measured on the oracle (64-cell sample, seed 3).
-CONFIG3_P0 = 1e-2
+UNEVEN_SOURCE_P0 = 1e-2
 # Straggler hand-off budget (FP64): cells past this many step attempts in one advance (about the p99
 # of this workload's step counts) finish on the cooperative kernel; the module's default.
-CONFIG3_BUDGET = 600
+UNEVEN_HANDOFF_BUDGET = 600
 
 
-def run_config3(args):
+def run_uneven_stiffness(args):
     import simstack_gb300 as sg
 
     cells = args.cells if args.cells != (1 << 20) else 262144
     duration = args.duration if args.duration != 10.0 else 60.0
     L = sg.lib()
     z = sg.air_cells(cells, seed=args.seed)
-    power = sg.air_source(z, seed=args.seed, P0=CONFIG3_P0, decades=3.0)
+    power = sg.air_source(z, seed=args.seed, P0=UNEVEN_SOURCE_P0, decades=3.0)
     mod = sg.Module(0, 3 * z.nbytes + (256 << 20))
     mod.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
     pristine = mod.upload(z)
@@ -578,7 +584,7 @@ def run_config3(args):
     zf = None
     for prec in (0, 2):
         launch.precision = prec
-        for kind, budget in ((0, 0), (2, 0), (2, CONFIG3_BUDGET)) if prec == 0 else ((0, 0), (2, 0)):
+        for kind, budget in ((0, 0), (2, 0), (2, UNEVEN_HANDOFF_BUDGET)) if prec == 0 else ((0, 0), (2, 0)):
             mod.set_straggler_budget(budget)
             sg.check(L.gpu_copy_on_device(work, pristine, z.nbytes), "copy")
             t = mod.autotune(launch, kind=kind)
@@ -607,7 +613,7 @@ def run_config3(args):
                 with np.errstate(all="ignore"):
                     rel = (np.abs(a - b) / np.abs(b))[sig]
                 results[key]["rel_err_vs_fp64"] = {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99))}
-    mod.set_straggler_budget(CONFIG3_BUDGET)
+    mod.set_straggler_budget(UNEVEN_HANDOFF_BUDGET)
     steps = zf["steps"][:cells]   # FP64 path: the oracle's step counts
     best = min((k for k in results if k.startswith("mixed")), key=lambda k: results[k]["ms"])
     line = {"metric": "cell-integrations/s", "value": results[best]["value"], "unit": "cell-integrations/s",
@@ -615,7 +621,7 @@ def run_config3(args):
             "headline_kernel": best,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"uneven stiffness: shipped mechanism, {cells} cells x {duration:g} s, averaged discharge "
-                                   f"source at P0 x 10^U[0,3] W/cm^3, P0 = {CONFIG3_P0:g}",
+                                   f"source at P0 x 10^U[0,3] W/cm^3, P0 = {UNEVEN_SOURCE_P0:g}",
                        "power_W_cm3": [float(power[:cells].min()), float(power[:cells].max())]},
             "accepted_steps_per_cell": {"min": float(steps.min()), "p50": float(np.median(steps)),
                                         "p99": float(np.quantile(steps, 0.99)), "max": float(steps.max())},
@@ -626,7 +632,7 @@ def run_config3(args):
     print(json.dumps(line))
 
 
-def run_config4(args):
+def run_large_mechanism(args):
     """Large synthetic mechanism through the cooperative kernels: mixed on --cells cells (default 65,536),
     FP64 (bit-identical to the reference's algorithm) on the first --fp64-cells of them."""
     import simstack_gb300 as sg
@@ -729,7 +735,7 @@ def serve_sample(seed: int, count: int, rate_hz: float = 200.0):
                  velocity=float(v[i]), seed=seed * 1000 + i) for i in range(count)]
 
 
-def run_config5(args):
+def run_serving(args):
     """Serving: requests submitted at their arrival times through the public serving API
     (host arrays in, results back on the host), the engine driven until every request is done."""
     import time
@@ -837,14 +843,14 @@ if __name__ == "__main__":
     a = parse()
     if a.profile_case:
         run_profile_case(a)
-    elif a.workload == "config3" and a.impl == "ours":
-        run_config3(a)
-    elif a.workload == "config5" and a.impl == "ours":
-        run_config5(a)
-    elif a.workload == "config4" and a.impl == "ours":
-        run_config4(a)
+    elif a.workload == "uneven-262144x60s" and a.impl == "ours":
+        run_uneven_stiffness(a)
+    elif a.workload == "serve-poisson200" and a.impl == "ours":
+        run_serving(a)
+    elif a.workload == "mech200-65536x10s" and a.impl == "ours":
+        run_large_mechanism(a)
     else:
-        if a.workload == "config1":   # the reference's CPU-runnable case: 4,096 cells x 1 s
+        if a.workload == "air-4096x1s":   # the reference's CPU-runnable case: 4,096 cells x 1 s
             a.cells = 4096 if a.cells == (1 << 20) else a.cells
             a.duration = 1.0 if a.duration == 10.0 else a.duration
         if a.impl == "reference":

@@ -424,7 +424,7 @@ def air_cells(cells: int, seed: int = 1, first_cell: int = 0, pad_to: int = 8, T
 
 
 def air_source(z: ZoneBlock, seed: int, P0: float, decades: float = 3.0, first_cell: int = 0) -> np.ndarray:
-    """Config-3 averaged discharge source per cell into z['src']; returns power per cell."""
+    """Averaged discharge source (the uneven-stiffness workload) per cell into z['src']; returns power per cell."""
     src = np.zeros((17, z.padded))
     power = np.zeros(z.padded)
     y = np.ascontiguousarray(z["y"])

@@ -64,7 +64,7 @@ def main() -> None:
     out["rates_T"], out["rates_M"] = Ts, Ms
     out["rates_k"] = np.stack([O.ref_air_rate_constants(T, M) for T, M in zip(Ts, Ms)])
 
-    # 3. config-1 sample: 64 cells, 1 s, rtol 1e-4, f64x4 generated (the production CPU path)
+    # 3. humid-air sample: 64 cells, 1 s, rtol 1e-4, f64x4 generated (the production CPU path)
     z = sg.air_cells(64, seed=1)
     out.update(block_arrays(z, "c1_in_"))
     b = aligned_block(z)

@@ -51,7 +51,7 @@ def test_rate_constants(oracle_lib):
             np.testing.assert_allclose(got, want, rtol=5e-16, atol=0)
 
 
-def test_config1_sample_f64x4(oracle_lib):
+def test_air_64_cells_f64x4(oracle_lib):
     z = zone_from("c1_in_", 17, 44)
     oracle_lib.Mechanism.air().advance("rodas3", oracle_lib.control(**BENCH_CTL), z.as_dict(), z.padded, 0, z.padded, 1.0, 0, 1)
     assert_state(z, "c1_out_")

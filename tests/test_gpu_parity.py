@@ -30,8 +30,8 @@ def assert_bits(a, b, names=STATE):
 
 @pytest.mark.parametrize("kind,block,variant", [(0, 128, 0), (1, 128, 0), (2, 128, 0), (2, 256, 2)],
                          ids=["static", "queue", "cta-queue", "cta-queue-256"])
-def test_f64_bit_identical_config1(module, oracle_lib, kind, block, variant):
-    """4,096-cell config-1 inputs (1 s, rtol 1e-4): every output bit equal to the oracle."""
+def test_f64_bit_identical_4096_cells(module, oracle_lib, kind, block, variant):
+    """4,096 seeded humid-air cells (1 s, rtol 1e-4): every output bit equal to the oracle."""
     module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
     module.set_tuning(kind=kind, block=block, variant=variant)
     z = sg.air_cells(4096, seed=1)
@@ -234,7 +234,7 @@ def test_mixed_matches_model(module, oracle_lib, method, mixed_variant):
 
 @pytest.mark.parametrize("mixed_variant", [0, 1], indirect=True, ids=["fp64-refinement", "double-float-state"])
 def test_mixed_precision_accuracy(module, oracle_lib, mixed_variant):
-    """Mixed path vs the FP64 oracle on 4,096 config-1 cells (rtol 1e-4). Bounds
+    """Mixed path vs the FP64 oracle on 4,096 seeded humid-air cells (1 s, rtol 1e-4). Bounds
     (measured on the CPU models of the mixed paths: max 7.3e-5 both, p99 3.9e-7
     (variant 0) and 8.7e-7 (variant 1), floored max 3.1e-4 and 1.3e-3):
     species >= 1e-6 ppm: max rel err < 1e-4, p99 < 1e-6; every entry with the
