@@ -191,7 +191,8 @@ SGB_API int32_t gpu_kin_set_mode(uint32_t mode);
  * warps next to stiff ones. Same results as gpu_kin_advance for every lane. */
 SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_ms);
 
-/* gpu_kin_advance_async + gpu_kin_wait with the copies overlapped: lanes [0, lane_count) of the
+/* An addition built on gpu_api.h:99 (gpu_kin_advance_async) and :105 (gpu_kin_wait): the two
+ * with the copies overlapped: lanes [0, lane_count) of the
  * host block (page-locked for overlap) are split into `chunks` (1..16) column ranges; chunk c+1
  * uploads while chunk c integrates and chunk c-1 downloads its first mutable_rows rows. Same
  * results per cell; waits; total_ms = device time from the first upload to the last download. */
