@@ -543,7 +543,13 @@ SGB_API int32_t gpu_kin_advance_pipelined(const GpuKinLaunch *launch, void *host
     }
     if (e == cudaSuccess) e = cudaEventRecord(g.pipe_end, g.copy_out);
     if (e == cudaSuccess) e = cudaEventSynchronize(g.pipe_end);
-    if (e != cudaSuccess) return (int32_t)e;
+    if (e != cudaSuccess) {   // nothing may still be copying into the caller's block when it gets the error
+        cudaStreamSynchronize(g.copy_in);
+        cudaStreamSynchronize(g.stream);
+        cudaStreamSynchronize(g.kern2);
+        cudaStreamSynchronize(g.copy_out);
+        return (int32_t)e;
+    }
     if (total_ms) cudaEventElapsedTime(total_ms, g.pipe_begin, g.pipe_end);
     ++g.launches;
     e = read_error_flag();
