@@ -1,7 +1,9 @@
 // Exports of the GB300 kinetics module: the reference's 16-entry GPU C ABI
 // (src/gpu/gpu_api.h) plus the module's extra entry points. One device, one
 // module-owned non-blocking stream; every copy and kernel of the module is
-// ordered on it (the reference's rule, src/gpu/kernels.cu:333-348).
+// ordered on it (the reference's rule, src/gpu/kernels.cu:333-348), except in
+// gpu_kin_advance_pipelined, whose upload, download and second kernel streams
+// start after the module stream's earlier work and are drained before it returns.
 
 #include <cuda_runtime.h>
 #include <stdio.h>

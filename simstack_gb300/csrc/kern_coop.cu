@@ -1,15 +1,16 @@
 // Cooperative kernels for large mechanisms: one CTA integrates one cell at a
 // time (persistent CTAs take cells from a work queue), its threads splitting
 // every phase of the Rosenbrock step -- rates per reaction, RHS per species,
-// Jacobian per entry, elimination per (row, column) of each pivot, solves per
-// row of each column. The step control is the reference's
+// Jacobian per entry, elimination per (row, column) of each pivot (two pivots
+// per pass for an FP64 LU in global memory), solves per row of each column. The step control is the reference's
 // (src/sim/kinetics/kin_solver.h:189-345): every thread runs the scalar
 // controller on the same values, so its decisions are uniform across the CTA.
 //
 // Precision 0: FP64 throughout, the same bits as the reference's solver (each
 // element sees the reference's operations in the reference's order; see
-// coop.h). The dense LU lives in per-CTA global scratch (L2-resident); the
-// pattern bitmask, vectors and rates live in shared memory.
+// coop.h). The dense LU lives in per-CTA global scratch (L2-resident), or in
+// shared memory when it fits in 64 KB; the pattern bitmask, vectors and rates
+// live in shared memory.
 // Precision 2 (mixed): FP64 RHS, Jacobian, residual, state and control; the
 // LU and the triangular solves in FP32 with the dense LU in shared memory;
 // each stage solve refined with FP64 residual sweeps.
