@@ -77,13 +77,13 @@ struct Module {
     uint32_t mixed_variant = 1;    // precision 2: 0 FP64-residual refinement, 1 double-float state (default)
     uint64_t launches = 0;
     float last_ms = 0.0f;
-    // straggler hand-off: cells past `straggler_budget` step attempts in one launch are parked
-    // and finished by the cooperative kernel (one CTA per cell) on the same stream
     cudaStream_t copy_in = nullptr, copy_out = nullptr;   // pipelined advance: upload and download streams
     cudaStream_t kern2 = nullptr;                         // ... and a second kernel stream
     static constexpr int kMaxChunks = 16;
     cudaEvent_t ev_in[kMaxChunks] = {}, ev_kern[kMaxChunks] = {};
     cudaEvent_t pipe_begin = nullptr, pipe_end = nullptr, pipe_after = nullptr;
+    // straggler hand-off: cells past `straggler_budget` step attempts in one launch are parked
+    // and finished by the cooperative kernel (one CTA per cell) on the same stream
     uint32_t straggler_budget = 600;  // FP64 step attempts per launch before a cell is handed on
     uint32_t straggler_block = 128;   // threads per parked cell
     SuspendRec *d_suspend = nullptr;
