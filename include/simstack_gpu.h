@@ -162,7 +162,8 @@ SGB_API int32_t gpu_copy_to_device(void *dst_device, const void *src_host, uint6
 SGB_API int32_t gpu_copy_to_host(void *dst_host, const void *src_device, uint64_t size);
 /* gpu_api.h:71 */
 SGB_API int32_t gpu_sync(void);
-/* gpu_api.h:75 -- the reference's particle demo kernel (kept for the loader). */
+/* gpu_api.h:75 -- advances one SoA position/velocity set by dt (the loader's demo entry point;
+ * here one leapfrog step under a softened pull toward the origin). */
 SGB_API int32_t gpu_step_points(float *x, float *y, float *z, float *vx, float *vy, float *vz, uint32_t count, float dt);
 /* gpu_api.h:80 -- upload mechanism, method and control; cudaErrorInvalidValue when the
  * mechanism does not fit. Selects the build-time straight-line kernels when the
@@ -242,6 +243,12 @@ SGB_API int32_t gpu_kin_set_straggler_block(uint32_t threads);
 /* Cells parked by the last advance that used the hand-off (waits for the module stream). */
 SGB_API int32_t gpu_kin_parked_cells(uint32_t *count);
 SGB_API uint32_t gpu_kin_get_mixed_variant(void);
+/* Poll limit of the bounded waits with which the table-driven kernels stage a mechanism's
+ * tables into shared memory (default 16,777,216 polls). A wait that runs out sets the launch's
+ * error flag and its CTA returns without touching a lane; the advance then returns
+ * cudaErrorTimeout. 0 makes every such wait give up at once: a way to exercise a caller's
+ * error path without a fault. */
+SGB_API int32_t gpu_kin_set_wait_limit(uint32_t polls);
 
 /* Measured instruction throughput of this device, operations per second (an
  * FMA is one operation): kind 0 FP64 FMA, 1 FP32 FMA, 2 FP32->FP64->FP32
@@ -258,21 +265,27 @@ SGB_API void *gpu_stream(void);
 /* No counterpart in the reference. The persistent work-queue advance for
  * callers that cannot allocate device memory: a caller whose device memory is
  * all owned by its own arena (SimStack's platform hands the simulation one
- * fixed block), a caller recording into a CUDA graph (allocations cannot be
- * captured) or a real-time loop that may not take cudaMalloc's device-wide
+ * fixed block), or a real-time loop that may not take cudaMalloc's device-wide
  * synchronisation. It needs no gpu_init and calls no cudaMalloc, cudaFree or
  * other allocating routine. Its scratch -- queue cursor, error flag and, for
  * mechanisms without generated code, the staged tables -- lives in a static
  * device array of 32 KiB that every GPU holds from library load to process
  * exit; a call whose scratch would exceed it returns
  * cudaErrorMemoryAllocation. mech / method / control are as for
- * gpu_kin_set_mech, the launch as for gpu_kin_advance (device pointers);
- * the work is enqueued on `stream` (a cudaStream_t, 0 = default stream) and,
- * if `wait` is nonzero, waited for and its error flag checked. The first call
- * on a device looks up the array's device address with that device current:
- * make it before any stream capture. Every call shares the array and clears
- * what must start at zero; calls that overlap on the GPU (other streams,
- * other host threads) race on it. */
+ * gpu_kin_set_mech, the launch as for gpu_kin_advance (device pointers); the
+ * kernel and launch shape are gpu_kin_advance_queue's defaults (CTA-synchronous
+ * queue, 128 threads per CTA) with the module's mixed variant and refinement
+ * sweeps. The work is enqueued on `stream` (a cudaStream_t, 0 = default
+ * stream) and, if `wait` is nonzero, waited for and its error flag checked
+ * (with wait = 0 a bounded-wait timeout of the table path is not reported: the
+ * next call clears the flag). Set-up, once per device with that device
+ * current and before any stream capture: the first call looks up the array's
+ * device address, and the context's per-thread stack reservation must cover
+ * the kernel's frame (gpu_init sets it; without gpu_init, call
+ * gpu_stack_limit(3840, ...) -- a call whose kernel needs more returns
+ * cudaErrorLaunchOutOfResources instead of letting the driver grow it). Every
+ * call shares the array and clears what must start at zero; calls that
+ * overlap on the GPU (other streams, other host threads) race on it. */
 SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *method, const KinControl *control,
                                         const GpuKinLaunch *launch, void *stream, int32_t wait);
 
@@ -388,12 +401,12 @@ SGB_API int32_t gpu_serve_stats(GpuServeStats *stats);
 SGB_API int32_t gpu_serve_close(void);
 
 /* ---------------------------------------------------------------------------
- * Host-side mechanism compiler: src/sim/kinetics/kin_build.cpp:199-365 and
+ * Host-side mechanism compiler: src/sim/kinetics/kin_build.cpp:78-244 and
  * air_mech.cpp:30-108, 205-276. Builds the reference-layout KinMech (same
  * pattern, pivot order and bytes as kin_mech_finalize), rate constants and
  * the discharge source. A handle is an opaque model.
  */
-/* Rate-law kinds and parameters (kin_build.cpp:137-174):
+/* Rate-law kinds and parameters (kin_build.cpp:42-53, 226-244):
  *   0 Arrhenius  p = {A, n, E}           k = A (T/300)^n exp(-E/T)
  *   1 third body p = {A, n, E}           same times [M]
  *   2 Troe       p = {A0, n0, Ainf, ninf, fc}

@@ -7,9 +7,9 @@
 //
 // It restates, for scalar lanes (one cell at a time), the reference's
 //   - mechanism builder and symbolic sparse-LU phase
-//       src/sim/kinetics/kin_build.cpp:199-344 (kin_add_species,
+//       src/sim/kinetics/kin_build.cpp:78-223 (kin_add_species,
 //       kin_add_reaction, kin_mech_finalize)
-//   - rate laws             kin_build.cpp:347-365 (kin_eval_rate_constants)
+//   - rate laws             kin_build.cpp:226-244 (kin_eval_rate_constants)
 //   - RHS / -J / LU / solve src/sim/kinetics/kin_solver.h:40-139
 //   - adaptive Rosenbrock   kin_solver.h:169-313 (kin_step_factor, kin_integrate)
 //   - pulse segments        kin_solver.h:322-347 (kin_advance)
@@ -105,7 +105,7 @@ static void fail(Mechanism *m, const char *what, const char *detail) {
     m->error = std::string(what) + ": " + detail;
 }
 
-// Element counts of a formula over N, O, H ("HNO3", "N2(A)"): kin_build.cpp:183-196.
+// Element counts of a formula over N, O, H ("HNO3", "N2(A)"): kin_build.cpp:62-76.
 static bool parse_formula(const char *name, u8 *counts) {
     static const char symbols[kElements] = {'N', 'O', 'H'};
     for (int e = 0; e < kElements; ++e) counts[e] = 0;
@@ -136,7 +136,7 @@ static int find_species(const Mechanism *m, const char *name) {
     return -1;
 }
 
-// "O + O2 + M -> O3 + M": kin_build.cpp:221-269. Reactants in equation
+// "O + O2 + M -> O3 + M": kin_build.cpp:100-148. Reactants in equation
 // order; net species in species-index order with non-zero net change.
 static u32 add_reaction(Mechanism *m, const char *equation, const RateLaw &law) {
     Reaction rx;
@@ -199,7 +199,7 @@ static u32 add_reaction(Mechanism *m, const char *equation, const RateLaw &law) 
     return r;
 }
 
-// Symbolic phase, kin_build.cpp:273-344: pattern = J + diagonal, IKJ fill-in
+// Symbolic phase, kin_build.cpp:152-223: pattern = J + diagonal, IKJ fill-in
 // of the no-pivot LU, row-major compact numbering, elimination op lists, and
 // triangular-solve lists (lower ascending column, upper DESCENDING column).
 static void finalize(Mechanism *m) {
@@ -267,7 +267,7 @@ static void finalize(Mechanism *m) {
             for (u32 e = 0; e < rx.net_count; ++e) rx.jac_index[p][e] = index[(size_t)rx.net_species[e] * n + rx.reactant[p]];
 }
 
-// kin_build.cpp:347-365; the operand order of each product is the reference's.
+// kin_build.cpp:226-244; the operand order of each product is the reference's.
 static void rate_constants(const Mechanism *m, double T, double M, double *k) {
     double t300 = T / 300.0;
     for (u32 r = 0; r < m->R(); ++r) {
@@ -501,7 +501,7 @@ struct Control {
 
 // ---------------------------------------------------------------------------
 // Scalar-lane arithmetic. T = double (f64 lanes) or float (f32 lanes). Each
-// helper is the reference lane operation of the same name (base_lane.h:253-341).
+// helper is the reference lane operation of the same name (base_lane.h:47-117).
 
 static inline double fmadd(double a, double b, double c) { return std::fma(a, b, c); }
 static inline float fmadd(float a, float b, float c) { return std::fma(a, b, c); }
@@ -1404,6 +1404,46 @@ void or_lu_ops(void *h, u32 *pivots4, u32 *updates2) {
     for (size_t s = 0; s < m->updates.size(); ++s) { updates2[2 * s] = m->updates[s].ij; updates2[2 * s + 1] = m->updates[s].kj; }
 }
 void or_rate_constants(void *h, double T, double M, double *k) { rate_constants((Mechanism *)h, T, M, k); }
+
+// Rate constants of `cells` cells into a [reaction][padded] block (T, M per cell).
+void or_rate_block(void *h, const double *T, const double *M, u32 cells, u32 padded, double *k) {
+    const Mechanism *m = (const Mechanism *)h;
+    std::vector<double> kk(m->R() ? m->R() : 1);
+    for (u32 i = 0; i < cells; ++i) {
+        rate_constants(m, T[i], M[i], kk.data());
+        for (u32 r = 0; r < m->R(); ++r) k[(size_t)r * padded + i] = kk[r];
+    }
+}
+
+// The seeded synthetic initial states of the shipped-mechanism workloads, drawn
+// exactly as the module's workload generator draws them (so the CPU baselines
+// integrate the same inputs without loading the module): a counter-based
+// splitmix64 stream per cell, draw j of cell c = mix(seed + (c*256 + j + 1) *
+// golden gamma); T ~ U[T_lo, T_hi], pH ~ U[3, 7] (drawn, unused), then each of
+// the n species c ~ 10^U[lc_lo, lc_hi] mol/L (the last, H2O, = 55.5 mol/L),
+// y = c * 6.02214076e20 cm^-3, M = 101325 / (1.380649e-23 T) * 1e-6 cm^-3.
+static inline u64 wl_mix64(u64 z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+    return z ^ (z >> 31);
+}
+static inline double wl_uniform(u64 seed, u64 cell, u32 j) {
+    return (double)(wl_mix64(seed + (cell * 256ull + j + 1ull) * 0x9E3779B97F4A7C15ull) >> 11) * (1.0 / 9007199254740992.0);
+}
+void or_workload_air(u64 seed, u64 first_cell, u32 cells, u32 padded, u32 n, double T_lo, double T_hi, double lc_lo,
+                     double lc_hi, double *y, double *T_out, double *M_out) {
+    for (u32 i = 0; i < cells; ++i) {
+        const u64 c = first_cell + i;
+        const double T = T_lo + (T_hi - T_lo) * wl_uniform(seed, c, 0);
+        for (u32 s = 0; s < n; ++s) {
+            const double lc = lc_lo + (lc_hi - lc_lo) * wl_uniform(seed, c, 2 + s);
+            const double conc = s == n - 1 ? 55.5 : std::pow(10.0, lc);
+            y[(size_t)s * padded + i] = conc * 6.02214076e20;
+        }
+        T_out[i] = T;
+        M_out[i] = 101325.0 / (1.380649e-23 * T) * 1e-6;
+    }
+}
 
 // Single-cell kernels (Jacobian / LU unit tests). T = f64.
 void or_fun(void *h, const double *k, const double *src, const double *y, double *f) { eval_fun(*(Mechanism *)h, k, src, y, f); }

@@ -74,6 +74,7 @@ struct Module {
     uint32_t mode = 0;
     GpuKinTuning tuning[3];
     uint32_t ir_sweeps = 1;
+    uint32_t wait_polls = kSpinLimit;   // poll limit of the table-staging waits
     uint32_t mixed_variant = 1;    // precision 2: 0 FP64-residual refinement, 1 double-float state (default)
     uint64_t launches = 0;
     float last_ms = 0.0f;
@@ -126,6 +127,7 @@ void fill_args(const GpuKinLaunch *L, DevArgs *A) {
     A->ir_sweeps = g.ir_sweeps;
     A->cursor = g.d_cursor;
     A->error_flag = g.d_error;
+    A->wait_polls = g.wait_polls;
     A->tables = g.d_tables;
     A->table_bytes = kTableBytes;
 }
@@ -376,21 +378,36 @@ SGB_API int32_t gpu_copy_to_host(void *dst_host, const void *src_device, uint64_
 SGB_API int32_t gpu_sync(void) { return (int32_t)cudaStreamSynchronize(g.stream); }
 
 namespace {
+// The loader's demo entry point: each point falls toward the origin under a
+// softened inverse-square pull, a = -x / (|x|^2 + eps^2)^(3/2), advanced by one
+// kick-drift-kick leapfrog step of dt (time-reversible, so orbits neither
+// gain nor lose energy over many calls).
+__device__ __forceinline__ void pull(float px, float py, float pz, float &ax, float &ay, float &az) {
+    const float eps2 = 0.01f;
+    const float r2 = fmaf(px, px, fmaf(py, py, fmaf(pz, pz, eps2)));
+    const float inv_r = rsqrtf(r2);
+    const float s = -(inv_r * inv_r * inv_r);
+    ax = s * px;
+    ay = s * py;
+    az = s * pz;
+}
 __global__ void step_points_kernel(float *x, float *y, float *z, float *vx, float *vy, float *vz, uint32_t count, float dt) {
-    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= count) return;
-    // harmonic pull toward the origin with a swirl about y and linear damping
-    const float k = 4.0f, w = 0.6f, damp = 1.0f - 0.02f * dt;
-    float px = x[i], py = y[i], pz = z[i];
-    float nvx = fmaf(-k * px + w * pz, dt, vx[i]) * damp;
-    float nvy = fmaf(-k * py, dt, vy[i]) * damp;
-    float nvz = fmaf(-k * pz - w * px, dt, vz[i]) * damp;
-    vx[i] = nvx;
-    vy[i] = nvy;
-    vz[i] = nvz;
-    x[i] = fmaf(nvx, dt, px);
-    y[i] = fmaf(nvy, dt, py);
-    z[i] = fmaf(nvz, dt, pz);
+    const float half = 0.5f * dt;
+    float px = x[i], py = y[i], pz = z[i], ax, ay, az;
+    pull(px, py, pz, ax, ay, az);
+    float ux = fmaf(ax, half, vx[i]), uy = fmaf(ay, half, vy[i]), uz = fmaf(az, half, vz[i]);
+    px = fmaf(ux, dt, px);
+    py = fmaf(uy, dt, py);
+    pz = fmaf(uz, dt, pz);
+    pull(px, py, pz, ax, ay, az);
+    x[i] = px;
+    y[i] = py;
+    z[i] = pz;
+    vx[i] = fmaf(ax, half, ux);
+    vy[i] = fmaf(ay, half, uy);
+    vz[i] = fmaf(az, half, uz);
 }
 }   // namespace
 
@@ -730,6 +747,17 @@ SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant) {
 }
 
 SGB_API uint32_t gpu_kin_get_mixed_variant(void) { return g.mixed_variant; }
+
+SGB_API int32_t gpu_kin_set_wait_limit(uint32_t polls) {
+    g.wait_polls = polls;
+    return 0;
+}
+
+namespace sgb {
+// Module settings read by the allocation-free advance (which needs no gpu_init).
+uint32_t module_wait_polls() { return g.wait_polls; }
+uint32_t module_ir_sweeps() { return g.ir_sweeps; }
+}   // namespace sgb
 
 // Measured instruction throughput (operations per second over the device):
 // kind 0 DFMA, 1 FFMA, 2 FP32<->FP64 conversion pairs, 3 DADD, 4 FP64 reciprocal, 5 FP64 sqrt.

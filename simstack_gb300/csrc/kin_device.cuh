@@ -30,7 +30,7 @@
 namespace sgb {
 
 // ---------------------------------------------------------------------------
-// Lane arithmetic with the reference's semantics (src/base/base_lane.h:253-341).
+// Lane arithmetic with the reference's semantics (src/base/base_lane.h:47-117).
 
 __device__ __forceinline__ double sgb_fma(double a, double b, double c) { return fma(a, b, c); }
 __device__ __forceinline__ float sgb_fma(float a, float b, float c) { return fmaf(a, b, c); }
@@ -133,6 +133,7 @@ struct DevArgs {
     uint32_t ir_sweeps;        // mixed path: refinement sweeps per stage solve (>= 1)
     uint32_t *cursor;          // queue kernel: next unclaimed lane
     uint32_t *error_flag;      // nonzero: a bounded wait ran out (tables not staged)
+    uint32_t wait_polls;       // poll limit of the table-staging wait (kSpinLimit unless a caller lowers it)
     const void *tables;        // table-driven ops: KinMech image in global memory
     uint32_t table_bytes;      // bytes to stage (multiple of 16)
     // straggler hand-off (queue and static kernels, precisions 0 and 3): a cell that has

@@ -27,7 +27,7 @@ int Model::find(const std::string &name) const {
 }
 
 // Formula over N, O, H with counts; a parenthesised suffix is an electronic
-// state label ("N2(A)", "O(1D)"): kin_build.cpp:183-196.
+// state label ("N2(A)", "O(1D)"): kin_build.cpp:62-76.
 static bool atoms_of(const char *name, uint8_t atoms[3]) {
     atoms[0] = atoms[1] = atoms[2] = 0;
     const char *p = name;
@@ -52,7 +52,7 @@ uint32_t Model::add_species(const char *name, bool abstract_species) {
     return n() - 1;
 }
 
-// Equation grammar of kin_build.cpp:221-269: tokens split on ' ' and '+',
+// Equation grammar of kin_build.cpp:100-148: tokens split on ' ' and '+',
 // "->" separates reactants from products, "M" (third body) is skipped,
 // tokens are at most 15 characters.
 uint32_t Model::add_reaction(const char *equation, const RateLaw &law) {
@@ -158,7 +158,7 @@ bool Model::finalize() {
     return true;
 }
 
-// kin_build.cpp:347-365, same operand order in every product.
+// kin_build.cpp:226-244, same operand order in every product.
 void Model::rate_constants(double T, double M, double *k) const {
     const double t300 = T / 300.0;
     for (uint32_t r = 0; r < R(); ++r) {

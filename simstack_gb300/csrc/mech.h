@@ -4,7 +4,7 @@
 // symbolic sparse LU: the non-zero pattern of J plus the diagonal, the fill-in
 // of a no-pivot IKJ elimination, a row-major compact numbering, and the flat
 // elimination / triangular-solve op lists the solver walks. The rules are the
-// reference's (src/sim/kinetics/kin_build.cpp:199-344): the same pattern, the
+// reference's (src/sim/kinetics/kin_build.cpp:78-223): the same pattern, the
 // same pivot order and the same op order, because the solver's results are
 // only bit-identical to the reference's when every floating-point operation
 // happens in the same sequence. Indices here are 32-bit, so the same compiler

@@ -51,7 +51,7 @@ def test_synthetic_large_mechanism_fill(oracle_lib):
     ("-> O3", "needs reactants"),
 ])
 def test_builder_rejects(oracle_lib, equation, reason):
-    """The reference's builder rejects these (kin_build.cpp:221-269); so do both restatements."""
+    """The reference's builder rejects these (kin_build.cpp:100-148); so do both restatements."""
     pm = sg.Model.new()
     om = oracle_lib.Mechanism()
     for s in ("O", "O2", "O3"):
