@@ -222,32 +222,68 @@ def measured_hbm_peak():
 
 
 # ---------------------------------------------------------------------------
-# CPU baseline: the reference algorithm (oracle restatement) on the host cores
+# CPU baseline: the reference's own CPU solver on the host cores. Neither this leg nor the
+# reference arm loads the GPU module: inputs come from oracle.air_block (the same seeded draws,
+# rate constants from the reference's kin_eval_rate_constants), and the timed work is the
+# reference's dbd_advance_threads (f64x4 lanes, generated AirGenOps, ~4 lane chunks per
+# thread, dbd.cpp:213-250) compiled from its sources into oracle/_ref/ -- scalar lanes
+# (SIM_SIMD=0) on an aarch64 host, where the reference's AVX2 lanes do not exist. Where
+# oracle/_ref could not be built, the oracle restatement (bit-identical to it) stands in.
 
-def cpu_baseline(cells_total: int, duration: float, seed: int, target_s: float, first_cell: int = 0):
-    import simstack_gb300 as sg
+def _cpu_advance(kind: str, block: dict, padded: int, duration: float, threads: int) -> float:
+    from oracle import oracle as O
+
+    t0 = time.perf_counter()
+    if kind == "reference":
+        O.ref_air_advance_threads("rodas3", O.control(), block, padded, 0, padded, duration, threads)
+    else:
+        O.Mechanism.air().advance("rodas3", O.control(), block, padded, 0, padded, duration, 0, threads)
+    return time.perf_counter() - t0
+
+
+def cpu_kind() -> str:
     from oracle import oracle as O
 
     O.build()
-    mech = O.Mechanism.air()
-    threads = os.cpu_count() or 1
-    # calibrate on a small sample, then size the timed sample to ~target_s
-    probe_cells = max(64, 8 * threads)
-    z = sg.air_cells(probe_cells, seed=seed, first_cell=first_cell)
-    t0 = time.perf_counter()
-    mech.advance("rodas3", O.control(), z.as_dict(), z.padded, 0, probe_cells, duration, 0, threads)
-    per_cell = (time.perf_counter() - t0) / probe_cells
+    return "reference" if O.ref_available() else "port"
+
+
+def cpu_sample_cells(kind: str, cells_total: int, duration: float, seed: int, target_s: float, threads: int) -> int:
+    """Cells (a multiple of 64) of the workload the CPU integrates in about target_s."""
+    from oracle import oracle as O
+
+    probe_cells = max(64, 8 * threads) // 8 * 8
+    block, P, _ = O.air_block(probe_cells, seed=seed)
+    per_cell = _cpu_advance(kind, block, P, duration, threads) / probe_cells
     cells = int(min(cells_total, max(probe_cells, target_s / max(per_cell, 1e-9))))
-    cells = max(64, cells // 64 * 64)
-    z = sg.air_cells(cells, seed=seed, first_cell=first_cell)
-    t0 = time.perf_counter()
-    mech.advance("rodas3", O.control(), z.as_dict(), z.padded, 0, cells, duration, 0, threads)
-    wall = time.perf_counter() - t0
-    return {"value": cells / wall, "unit": "cell-integrations/s", "cores": threads, "kind": "port",
-            "sample": f"first {cells} cells of the workload (same seeded inputs), {duration:g} s each, "
-                      f"{threads} host threads, {wall:.1f} s wall; oracle/kin_oracle.cpp (the reference's FP64 "
-                      f"algorithm, bit-identical to its CPU path)",
-            "wall_s": wall, "cells": cells}
+    return max(64, cells // 64 * 64)
+
+
+import platform as _platform
+
+CPU_PATHS = {"reference": "the reference's dbd_advance_threads<f64x4, AirGenOps> compiled from its sources "
+                          + ("(oracle/_ref; AVX2 lanes, SIM_SIMD=1)" if _platform.machine() == "x86_64" else
+                             f"(oracle/_ref; portable scalar lanes, SIM_SIMD=0: {_platform.machine()} has no AVX2)"),
+             "port": "oracle/kin_oracle.cpp, the reference's FP64 algorithm restated (bit-identical to its CPU path)"}
+
+
+def cpu_baseline(cells_total: int, duration: float, seed: int, target_s: float, with_port: bool = True):
+    from oracle import oracle as O
+
+    kind = cpu_kind()
+    threads = os.cpu_count() or 1
+    cells = cpu_sample_cells(kind, cells_total, duration, seed, target_s, threads)
+    block, P, rates = O.air_block(cells, seed=seed)
+    wall = _cpu_advance(kind, block, P, duration, threads)
+    out = {"value": cells / wall, "unit": "cell-integrations/s", "cores": threads, "kind": kind,
+           "sample": f"first {cells} cells of the workload (same seeded inputs), {duration:g} s each, {threads} host "
+                     f"threads, {wall:.1f} s wall; {CPU_PATHS[kind]}; rate constants from the {rates}",
+           "wall_s": wall, "cells": cells}
+    if with_port and kind == "reference":   # the restatement on the same sample, for comparison
+        block, P, _ = O.air_block(cells, seed=seed)
+        wall_p = _cpu_advance("port", block, P, duration, threads)
+        out["port"] = {"value": cells / wall_p, "kind": "port", "cores": threads, "sample": CPU_PATHS["port"]}
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -268,35 +304,37 @@ def air_workload(cells: int, duration: float) -> str:
 
 
 def run_reference(args):
+    """The reference's own CPU path on the host cores (rank 0 only), on a bounded sample of the
+    workload per step. Loads only oracle/ libraries: no GPU module, no simstack_gb300 code."""
     world, rank, local = dist_env()
     if rank != 0:
         return
-    cb = cpu_baseline(args.cells, args.duration, args.seed, args.cpu_seconds)
-    # `steps` timed samples of the same bounded workload, after warm-up
-    import simstack_gb300 as sg
     from oracle import oracle as O
 
-    mech = O.Mechanism.air()
-    cells, threads = cb["cells"], cb["cores"]
+    kind = cpu_kind()
+    threads = os.cpu_count() or 1
+    cells_total, duration = args.cells, args.duration
+    if args.workload == "air-4096x1s":
+        cells_total, duration = 4096, 1.0
+    per_step_s = max(1.0, args.cpu_seconds / max(args.steps, 1))
+    cells = cpu_sample_cells(kind, cells_total, duration, args.seed, per_step_s, threads)
     times = []
     for it in range(args.warmup + args.steps):
+        block, P, rates = O.air_block(cells, seed=args.seed)
         if it < args.warmup and it > 0:
             continue   # the calibration run above already warmed the caches
-        z = sg.air_cells(cells, seed=args.seed)
-        t0 = time.perf_counter()
-        mech.advance("rodas3", O.control(), z.as_dict(), z.padded, 0, cells, args.duration, 0, threads)
-        times.append(time.perf_counter() - t0)
+        times.append(_cpu_advance(kind, block, P, duration, threads))
     times = times[-args.steps:]
     value = cells / float(np.mean(times))
+    sample = (f"each step integrates the first {cells} of the {cells_total} cells (bounded CPU sample), {threads} host "
+              f"threads; {CPU_PATHS[kind]}; rate constants from the {rates}; value = cells per second of that sample")
     line = {"metric": "cell-integrations/s", "value": value, "unit": "cell-integrations/s", "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup, "ms_per_step": float(np.mean(times)) * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": air_workload(args.cells, args.duration), "cells_per_gpu": args.cells,
-                       "duration_s": args.duration, "precision": "f64",
-                       "sample": f"each step integrates the first {cells} of the {args.cells} cells (bounded CPU sample); "
-                                 f"value = cells per second of that sample"},
-            "cpu_baseline": {"value": value, "unit": "cell-integrations/s", "cores": threads, "kind": "port",
-                             "sample": cb["sample"]},
+            "config": {"workload": air_workload(cells_total, duration), "cells_per_gpu": cells_total,
+                       "duration_s": duration, "precision": "f64", "sample": sample},
+            "cpu_baseline": {"value": value, "unit": "cell-integrations/s", "cores": threads, "kind": kind,
+                             "sample": sample},
             "e2e": {"value": value, "unit": "cell-integrations/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
 

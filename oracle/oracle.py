@@ -118,6 +118,8 @@ def lib() -> C.CDLL:
         L.or_advect.argtypes = [vp, u32, u32, u32, vp, d, u32]
         L.or_fnv1a.argtypes = [vp, u64]
         L.or_fnv1a.restype = u64
+        L.or_rate_block.argtypes = [vp, vp, vp, u32, u32, vp]
+        L.or_workload_air.argtypes = [u64, u64, u32, u32, u32, d, d, d, d, vp, vp, vp]
         _lib = L
     return _lib
 
@@ -249,6 +251,34 @@ def advect(x: np.ndarray, inlet: np.ndarray, courant: float, substeps: int) -> N
     lib().or_advect(_ptr(x), x.shape[0], x.shape[1], x.shape[1], _ptr(inlet), courant, substeps)
 
 
+def air_block(cells: int, seed: int = 1, first_cell: int = 0, pad_to: int = 8, T=(288.0, 303.0),
+              log10_c=(-12.0, -2.0), rates: str = "reference"):
+    """The shipped-mechanism workload as a zone block (dict of 64-byte aligned float64 rows,
+    `padded` lanes), built without the GPU module: the same seeded draws as the module's
+    workload generator, rate constants from the reference's own kin_eval_rate_constants
+    (oracle/_ref) when rates == "reference" and it was built, else from the oracle's
+    restatement of it. Padding lanes copy cell 0. Returns (block, padded, rates_used)."""
+    n, R = 17, 44
+    P = max(pad_to, (cells + pad_to - 1) // pad_to * pad_to)
+    block = {"y": aligned_zeros((n, P)), "k": aligned_zeros((R, P)), "src": aligned_zeros((n, P)),
+             "pulse": aligned_zeros((n, P))}
+    for name in ("h", "steps", "rejects", "pulses", "failed", "period", "pulse_first", "pulse_count"):
+        block[name] = aligned_zeros(P)
+    T_v, M_v = np.zeros(P), np.zeros(P)
+    lib().or_workload_air(seed, first_cell, cells, P, n, T[0], T[1], log10_c[0], log10_c[1], _ptr(block["y"]),
+                          _ptr(T_v), _ptr(M_v))
+    used = "reference" if rates == "reference" and ref_available() else "oracle"
+    if used == "reference":
+        ref().ref_air_rate_block(_ptr(T_v), _ptr(M_v), cells, P, _ptr(block["k"]))
+    else:
+        m = Mechanism.air()
+        lib().or_rate_block(m.h, _ptr(T_v), _ptr(M_v), cells, P, _ptr(block["k"]))
+    for i in range(cells, P):
+        block["y"][:, i] = block["y"][:, 0]
+        block["k"][:, i] = block["k"][:, 0]
+    return block, P, used
+
+
 def fnv1a(data: bytes) -> int:
     buf = np.frombuffer(data, np.uint8).copy()
     return int(lib().or_fnv1a(_ptr(buf), len(buf)))
@@ -279,6 +309,9 @@ def ref() -> C.CDLL:
         L.ref_air_advance.restype = i32
         L.ref_robertson.argtypes = [i32, C.POINTER(Control), d, vp, vp]
         L.ref_robertson.restype = i32
+        L.ref_air_rate_block.argtypes = [vp, vp, u32, u32, vp]
+        L.ref_air_advance_threads.argtypes = [i32, C.POINTER(Control), C.POINTER(LaneArrays), u32, u32, d, u32]
+        L.ref_air_advance_threads.restype = i32
         _ref = L
     return _ref
 
@@ -312,6 +345,17 @@ def ref_air_advance(method: str, ctl: Control, block: dict, padded: int, begin: 
     rc = ref().ref_air_advance(METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, REF_VARIANTS[variant])
     if rc != 0:
         raise RuntimeError(f"ref_air_advance: {rc}")
+
+
+def ref_air_advance_threads(method: str, ctl: Control, block: dict, padded: int, begin: int, end: int,
+                            duration: float, threads: int) -> None:
+    """Lanes [begin, end) (multiples of 8) through the reference's production CPU path,
+    dbd_advance_threads (f64x4 lanes, generated AirGenOps, ~4 lane chunks per thread),
+    on `threads` host threads."""
+    la = lane_arrays(block, padded)
+    rc = ref().ref_air_advance_threads(METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, threads)
+    if rc != 0:
+        raise RuntimeError(f"ref_air_advance_threads: {rc}")
 
 
 def ref_robertson(method: str, ctl: Control, t_end: float = 40.0):

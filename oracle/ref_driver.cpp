@@ -23,6 +23,10 @@ struct DebugTable;
 #include <stdlib.h>
 #include <math.h>
 
+#include <atomic>
+#include <thread>
+#include <vector>
+
 #include "sim_platform.h"
 #include "sim/dbd.cpp"
 
@@ -103,6 +107,71 @@ REF_API s32 ref_air_advance(s32 method_id, const RefControl *rc, const RefLaneAr
         case 4: dbd_advance_cpu<f32, AirGenOps, true>(&z, &model->mech, &method, &ctl, duration, first, end); break;
         default: return -1;
     }
+    return 0;
+}
+
+// Rate constants of `cells` cells from T and M per cell into a [reaction][padded] block:
+// the reference's kin_eval_rate_constants, cell by cell.
+REF_API void ref_air_rate_block(const f64 *T, const f64 *M, u32 cells, u32 padded, f64 *k) {
+    KinModel *model = air_model();
+    const u32 R = model->mech.reaction_count;
+    f64 kk[KIN_MAX_REACTIONS];
+    for (u32 i = 0; i < cells; ++i) {
+        kin_eval_rate_constants(model, T[i], M[i], kk);
+        for (u32 r = 0; r < R; ++r) k[(u64)r * padded + i] = kk[r];
+    }
+}
+
+// A work queue behind the reference's PlatformAPI (sim_platform.h:41-62), so the
+// reference's own threaded advance runs here unchanged: add_work_entry records an
+// entry, complete_all_work runs every recorded entry on `threads` threads (the
+// caller among them) and returns when all have finished.
+struct PlatformWorkQueue {
+    struct Entry { platform_work_queue_callback *fn; void *data; };
+    std::vector<Entry> entries;
+    u32 threads;
+};
+
+static PLATFORM_ADD_WORK_ENTRY(ref_add_work_entry) { queue->entries.push_back({callback, data}); }
+
+static PLATFORM_COMPLETE_ALL_WORK(ref_complete_all_work) {
+    std::atomic<u32> next{0};
+    const u32 count = (u32)queue->entries.size();
+    auto worker = [&]() {
+        for (u32 i = next.fetch_add(1); i < count; i = next.fetch_add(1)) queue->entries[i].fn(queue, queue->entries[i].data);
+    };
+    std::vector<std::thread> pool;
+    for (u32 t = 1; t < queue->threads; ++t) pool.emplace_back(worker);
+    worker();
+    for (std::thread &th : pool) th.join();
+    queue->entries.clear();
+}
+
+// Lanes [first, end) of a zone block through the reference's production CPU path,
+// dbd_advance_threads (dbd.cpp:213-250): f64x4 lanes with the generated AirGenOps,
+// about four contiguous lane chunks per thread, on `threads` host threads.
+REF_API s32 ref_air_advance_threads(s32 method_id, const RefControl *rc, const RefLaneArrays *a, u32 first, u32 end,
+                                    f64 duration, u32 threads) {
+    KinModel *model = air_model();
+    KinMethod method = kin_method((KinMethodId)method_id);
+    KinControl ctl = to_control(rc);
+    if (first % 8 || end % 8 || threads == 0) return -1;
+    DbdZones z = {};
+    z.padded = a->padded;
+    z.n_species = model->mech.species_count;
+    z.n_reactions = model->mech.reaction_count;
+    z.y = a->y; z.h = a->h; z.steps = a->steps; z.rejects = a->rejects; z.pulses = a->pulses; z.failed = a->failed;
+    z.k = (f64 *)a->k; z.src = (f64 *)a->src; z.pulse = (f64 *)a->pulse; z.period = (f64 *)a->period;
+    z.pulse_first = (f64 *)a->pulse_first; z.pulse_count = (f64 *)a->pulse_count;
+    PlatformAPI api = {};
+    api.add_work_entry = ref_add_work_entry;
+    api.complete_all_work = ref_complete_all_work;
+    PlatformWorkQueue queue;
+    queue.threads = threads;
+    static u8 frame_memory[1 << 20];
+    Arena frame = arena_make(frame_memory, sizeof(frame_memory));
+    dbd_advance_threads(&z, &model->mech, &method, &ctl, duration, 1, DbdPrecision_F64, &api, &queue, threads, &frame,
+                        first, end);
     return 0;
 }
 

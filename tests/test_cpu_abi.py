@@ -11,7 +11,8 @@ import pytest
 import simstack_gb300 as sg
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF_SRC = os.environ.get("SIMSTACK_REF_DIR", "/root/reference")
+# the reference sources: SIMSTACK_REF_DIR, else the staged copy (oracle/Makefile `stage`)
+REF_SRC = os.environ.get("SIMSTACK_REF_DIR", os.path.join(ROOT, "baseline", "_ref"))
 
 
 def declared_exports():

@@ -46,3 +46,18 @@ def test_rate_constants_and_source_match_reference(oracle_lib):
         y = 10.0 ** rng.uniform(6, 19, 17)
         e, T = 10.0 ** rng.uniform(-8, 1), rng.uniform(280, 420)
         assert np.array_equal(O.source_delta(y, e, T), O.ref_air_source_delta(y, e, T))
+
+
+def test_threaded_reference_path_and_module_free_inputs(oracle_lib):
+    """The CPU baselines' inputs (oracle.air_block: no GPU module) equal the module's workload
+    generator bit for bit, rate constants from the reference included; the reference's threaded
+    production path (dbd_advance_threads) gives the oracle's bits on them."""
+    b, P, used = O.air_block(1000, seed=9, first_cell=77)
+    z = sg.air_cells(1000, seed=9, first_cell=77)
+    assert used == "reference" and P == z.padded
+    for name in sg.ROWS_ORDER:
+        assert b[name].tobytes() == np.ascontiguousarray(z[name]).tobytes(), name
+    O.ref_air_advance_threads("rodas3", O.control(), b, P, 0, P, 1.0, 4)
+    O.Mechanism.air().advance("rodas3", O.control(), z.as_dict(), z.padded, 0, z.padded, 1.0, 0, 2)
+    for name in STATE:
+        assert z[name].tobytes() == b[name].tobytes(), name
