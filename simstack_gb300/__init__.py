@@ -158,6 +158,7 @@ def lib() -> C.CDLL:
             "gpu_kin_set_refinement": (i32, [u32]),
             "gpu_kin_set_mixed_variant": (i32, [u32]),
             "gpu_kin_get_mixed_variant": (u32, []),
+            "gpu_kin_set_wait_limit": (i32, [u32]),
             "gpu_kin_set_straggler_budget": (i32, [u32]),
             "gpu_kin_set_straggler_block": (i32, [u32]),
             "gpu_stack_limit": (i32, [u64, C.POINTER(u64)]),

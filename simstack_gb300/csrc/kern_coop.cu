@@ -1033,6 +1033,7 @@ SGB_API int32_t gpu_kin_coop_advance(const GpuKinLaunch *L, float *kernel_ms) {
     A.ir_sweeps = cm.ir_sweeps;
     A.cursor = cm.d_header;
     A.error_flag = cm.d_header + 32;
+    A.wait_polls = kSpinLimit;
     A.tables = cm.d_image;
     A.table_bytes = cm.head.bytes;
     if (A.lanes == 0 || A.duration == 0.0) {

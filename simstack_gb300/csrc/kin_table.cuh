@@ -38,7 +38,10 @@ struct TableOps {
             mbar_arrive_expect_tx(&bar, A.table_bytes);
             tma_bulk_g2s(smem, A.tables, A.table_bytes, &bar);
         }
-        bool ok = mbar_wait(&bar, 0);
+        const bool ok = mbar_wait(&bar, 0, A.wait_polls);
+        // on a timeout the copy may still be in flight into this CTA's shared memory:
+        // let it land (a second bounded wait) before the CTA gives up and exits
+        if (!ok) mbar_wait(&bar, 0);
         __syncthreads();
         return ok;
     }

@@ -1,7 +1,8 @@
 // Inline-PTX helpers for sm_103a: mbarrier and the TMA bulk copy
 // (cp.async.bulk) used to stage mechanism tables into shared memory.
-// Every wait is bounded: after kSpinLimit polls it reports failure instead
-// of spinning on, and the caller records an error and returns.
+// Every wait is bounded: after a poll limit (kSpinLimit by default, or the
+// launch's own limit) it reports failure instead of spinning on, and the
+// caller records an error and returns.
 
 #pragma once
 #include <stdint.h>
@@ -30,9 +31,10 @@ __device__ __forceinline__ void tma_bulk_g2s(void *dst, const void *src, uint32_
                  : "memory");
 }
 
-// Bounded wait for phase `parity` of `bar`; false if the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
-    for (uint32_t it = 0; it < kSpinLimit; ++it) {
+// Bounded wait for phase `parity` of `bar`: at most `polls` polls (0: none);
+// false if they ran out before the phase completed.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint32_t polls = kSpinLimit) {
+    for (uint32_t it = 0; it < polls; ++it) {
         uint32_t done;
         asm volatile(
             "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"

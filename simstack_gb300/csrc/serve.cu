@@ -281,6 +281,7 @@ cudaError_t admit(Request *r) {
     A.ir_sweeps = 1;
     A.cursor = (uint32_t *)r->d_scratch;
     A.error_flag = (uint32_t *)(r->d_scratch + 128);
+    A.wait_polls = kSpinLimit;
     A.tables = r->d_scratch + 256;
     A.table_bytes = kTableBytes;
 

@@ -3,20 +3,27 @@
 //
 // Who needs it: a caller that owns all device memory through its own arena
 // (SimStack's platform layer hands the simulation one fixed block and never
-// allocates again), a caller recording the advance into a CUDA graph (an
-// allocation cannot be captured), or a caller on a real-time loop that may not
-// take cudaMalloc's implicit device-wide synchronisation. gpu_init allocates
-// the module's arena and scratch, so such callers cannot use the regular
-// entry points; this one needs no gpu_init at all.
+// allocates again), or a caller on a real-time loop that may not take
+// cudaMalloc's implicit device-wide synchronisation. gpu_init allocates the
+// module's arena and scratch, so such callers cannot use the regular entry
+// points; this one needs no gpu_init.
 //
 // What it uses instead: the queue kernel's scratch -- the work-queue cursor,
 // the bounded-wait error flag and, for mechanisms without generated code, the
 // staged copy of the mechanism tables -- lives in g_kin_static_scratch below,
 // a file-scope device array of kStaticScratchBytes (32 KiB) that every GPU
 // holds from the moment the library is loaded until the process exits. The
-// kernels are the ones gpu_kin_advance_queue launches; only where their
+// kernel is the one gpu_kin_advance_queue launches at the module's default
+// launch shape (the CTA-synchronous persistent queue, 128 threads per CTA),
+// with the module's mixed-path variant and refinement setting; only where its
 // scratch lives differs. Inputs and outputs are the caller's zone block, as
 // for every other advance.
+//
+// Local memory: the context's per-thread stack reservation (cudaLimitStackSize)
+// must already cover the kernel's frame, since a launch that needs more makes
+// the driver grow the reservation -- a device allocation. gpu_init fixes it
+// once; a caller without gpu_init sets it with gpu_stack_limit at set-up. The
+// entry point checks it and returns cudaErrorLaunchOutOfResources otherwise.
 
 #include <cuda_runtime.h>
 #include <string.h>
@@ -44,7 +51,17 @@ cudaError_t launch_air_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
 cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
+cudaError_t local_air_p0(uint32_t, uint32_t, size_t *);
+cudaError_t local_air_p1(uint32_t, uint32_t, size_t *);
+cudaError_t local_air_p2(uint32_t, uint32_t, size_t *);
+cudaError_t local_air_p3(uint32_t, uint32_t, size_t *);
+cudaError_t local_table_p0(uint32_t, size_t *);
+cudaError_t local_table_p1(uint32_t, size_t *);
+cudaError_t local_table_p2(uint32_t, size_t *);
+cudaError_t local_table_p3(uint32_t, size_t *);
 uint64_t air_ops_signature();
+uint32_t module_wait_polls();
+uint32_t module_ir_sweeps();
 }   // namespace sgb
 
 using namespace sgb;
@@ -108,8 +125,9 @@ SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *me
     e = cudaMemsetAsync(scratch, 0, kQueueHeaderBytes, s);
     if (e != cudaSuccess) return (int32_t)e;
     if (!generated) {
-        // staged once per call from a host image (pageable: the copy is staged before this call returns)
-        static unsigned char image[kTableBytes];
+        // copied on every call from a per-host-thread image in pageable memory (the runtime has
+        // consumed it by the time cudaMemcpyAsync returns)
+        static thread_local unsigned char image[kTableBytes];
         table_image(mech, image);
         e = cudaMemcpyAsync(scratch + kQueueHeaderBytes, image, kTableBytes, cudaMemcpyHostToDevice, s);
         if (e != cudaSuccess) return (int32_t)e;
@@ -132,28 +150,40 @@ SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *me
     memcpy(A.new_f, method->new_f, sizeof(A.new_f));
     A.stages = method->stages;
     A.order = method->order;
-    A.ir_sweeps = 1;
+    A.ir_sweeps = module_ir_sweeps();
     A.cursor = (uint32_t *)scratch;
     A.error_flag = (uint32_t *)(scratch + 128);
+    A.wait_polls = module_wait_polls();
     A.tables = scratch + kQueueHeaderBytes;
     A.table_bytes = kTableBytes;
     if (A.lanes == 0) return 0;
+
+    // the module's default launch shape: CTA-synchronous persistent queue, 128 threads, 255 registers
+    const uint32_t kind = 2, variant = 0;
+    // precision 2 runs the module's current mixed variant (gpu_kin_set_mixed_variant)
+    const uint32_t p = L->precision == 2 && gpu_kin_get_mixed_variant() == 1 ? 3u : L->precision;
+    size_t frame = 0, reserved = 0;
+    if (generated) e = p == 0 ? local_air_p0(kind, variant, &frame) : p == 1 ? local_air_p1(kind, variant, &frame)
+                       : p == 2 ? local_air_p2(kind, variant, &frame) : local_air_p3(kind, variant, &frame);
+    else e = p == 0 ? local_table_p0(kind, &frame) : p == 1 ? local_table_p1(kind, &frame)
+             : p == 2 ? local_table_p2(kind, &frame) : local_table_p3(kind, &frame);
+    if (e == cudaSuccess) e = cudaDeviceGetLimit(&reserved, cudaLimitStackSize);
+    if (e != cudaSuccess) return (int32_t)e;
+    if (frame > reserved) return (int32_t)cudaErrorLaunchOutOfResources;   // the launch would grow the reservation
 
     int dev = 0, sms = 0, per_sm = 0;
     cudaGetDevice(&dev);
     e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return (int32_t)e;
     Shape sh;
-    sh.kind = 1;
+    sh.kind = kind;
     sh.block = 128;
-    sh.variant = 0;
+    sh.variant = variant;
     sh.smem = generated ? 0 : kTableBytes;
-    // precision 2 runs the module's current mixed variant (gpu_kin_set_mixed_variant)
-    const uint32_t p = L->precision == 2 && gpu_kin_get_mixed_variant() == 1 ? 3u : L->precision;
-    if (generated) e = p == 0 ? occupancy_air_p0(1, 0, sh.block, &per_sm) : p == 1 ? occupancy_air_p1(1, 0, sh.block, &per_sm)
-                       : p == 2 ? occupancy_air_p2(1, 0, sh.block, &per_sm) : occupancy_air_p3(1, 0, sh.block, &per_sm);
-    else e = p == 0 ? occupancy_table_p0(1, sh.block, sh.smem, &per_sm) : p == 1 ? occupancy_table_p1(1, sh.block, sh.smem, &per_sm)
-             : p == 2 ? occupancy_table_p2(1, sh.block, sh.smem, &per_sm) : occupancy_table_p3(1, sh.block, sh.smem, &per_sm);
+    if (generated) e = p == 0 ? occupancy_air_p0(kind, variant, sh.block, &per_sm) : p == 1 ? occupancy_air_p1(kind, variant, sh.block, &per_sm)
+                       : p == 2 ? occupancy_air_p2(kind, variant, sh.block, &per_sm) : occupancy_air_p3(kind, variant, sh.block, &per_sm);
+    else e = p == 0 ? occupancy_table_p0(kind, sh.block, sh.smem, &per_sm) : p == 1 ? occupancy_table_p1(kind, sh.block, sh.smem, &per_sm)
+             : p == 2 ? occupancy_table_p2(kind, sh.block, sh.smem, &per_sm) : occupancy_table_p3(kind, sh.block, sh.smem, &per_sm);
     if (e != cudaSuccess) return (int32_t)e;
     if (per_sm < 1) per_sm = 1;
     const uint32_t resident = (uint32_t)per_sm * (uint32_t)sms, needed_ctas = (A.lanes + sh.block - 1) / sh.block;
