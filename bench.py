@@ -47,6 +47,8 @@ WORKLOADS = {
     "uneven-262144x60s": "uneven stiffness: 262,144 cells x 60 s with a discharge source, static vs queue vs hand-off",
     "mech200-65536x10s": "200-species / 1,200-reaction synthetic mechanism, 65,536 cells x 10 s, one CTA per cell",
     "serve-poisson200": "served requests (Poisson arrivals at 200 req/s) with film advection, p50/p99 latency",
+    "dbd-sweep-4096": "the reference's 4,096-zone DBD sweep (64 x 64 power x humidity grid), 20 ms chemistry steps, "
+                      "pulsed and averaged: device-resident zone driver vs the per-step block upload, sim-s per wall-s",
 }
 
 
@@ -675,6 +677,131 @@ def run_uneven_stiffness(args):
     print(json.dumps(line))
 
 
+# The sweep scene (src/sim/dbd_scene.cpp:82-140): 64 x 64 zones at 310 K, 1 atm, 10 kHz,
+# power 0.01 x 50^fx W/cm^3 (log spaced to 0.5), x_H2O 0.04 fy; the sim's default chemistry
+# step of 20 ms (chem_steps 20 x 1 ms), dbd_default_control (dbd.cpp:485-495); f32 Delta lanes
+# are the sweep's default precision. The reference publishes 0.09 sim-s per wall-s for the
+# pulsed sweep on its CUDA path (RTX 3060) and 0.06 on 8 CPU cores (docs/M2_KINETICS.md:197-203).
+SWEEP_SIDE, SWEEP_DT = 64, 0.02
+SWEEP_PULSED_PUBLISHED_CUDA = 0.09
+
+
+def sweep_zones(side: int = SWEEP_SIDE):
+    import math
+
+    import simstack_gb300 as sg
+
+    n = side * side
+    fx = [(i % side) / (side - 1) for i in range(n)]
+    fy = [(i // side) / (side - 1) for i in range(n)]
+    power = np.array([0.01 * math.pow(50.0, v) for v in fx])
+    x_h2o = np.array([0.04 * v for v in fy])
+    return sg.dbd_zones(n, 310.0, x_h2o, power, 10000.0)
+
+
+def sweep_control():
+    import simstack_gb300 as sg
+
+    return sg.control(rtol=1e-3, atol=1e8, h_min=1e-14, h_start=1e-9, max_steps=20000)
+
+
+def run_dbd_sweep(args):
+    """Sim-seconds per wall-second of the 4,096-zone sweep: the device-resident zone driver
+    (gpu_dbd_step: source, advance, commit on the device, nothing copied between master steps)
+    against the reference's own call pattern through this module's C ABI (host-side source and
+    commit, the whole block uploaded and the solver rows downloaded around every advance,
+    dbd.cpp:272-295), and the reference's own threaded CPU sweep (oracle/_ref)."""
+    import ctypes as C
+
+    import simstack_gb300 as sg
+
+    L = sg.lib()
+    mod = sg.Module(0, 1 << 30)
+    mod.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sweep_control())
+    results = {}
+    steps_for = {"pulsed": max(2, args.steps), "averaged": max(10, 5 * args.steps)}
+    clocks = ClockSampler(0)
+    clocks.start()
+    for mode, nsteps in steps_for.items():
+        pulsed = mode == "pulsed"
+        for prec, pname in ((1, "f32"), (0, "f64"), (2, "mixed")):
+            # device-resident: one upload, then gpu_dbd_step per master step
+            z = sweep_zones()
+            dev = sg.DeviceZones(mod, z)
+            dev.step(0.0, SWEEP_DT, pulsed, precision=prec)   # warm-up step (kernels loaded, tuning in place)
+            dev = sg.DeviceZones(mod, sweep_zones())
+            t, dev_ms = 0.0, []
+            sg.check(L.gpu_sync(), "sync")
+            w0 = time.perf_counter()
+            for _ in range(nsteps):
+                dev_ms.append(dev.step(t, SWEEP_DT, pulsed, precision=prec))
+                t = t + SWEEP_DT
+            wall_dev = time.perf_counter() - w0
+            got = dev.download().copy()
+            # the reference's call pattern: host source + commit, block up, advance, solver rows down
+            z = sweep_zones()
+            base = mod.alloc(z.nbytes)
+            sg.check(L.gpu_host_register(z.data.ctypes.data, z.nbytes), "gpu_host_register")
+            launch = z.launch(base, prec, SWEEP_DT)
+            t, ref_wall = 0.0, 0.0
+            for _ in range(nsteps):
+                sg.dbd_prepare_source(z, pulsed, t, t + SWEEP_DT)          # host, outside the timer
+                w0 = time.perf_counter()
+                sg.check(L.gpu_copy_to_device(base, z.data.ctypes.data, z.nbytes), "up")
+                ms = C.c_float()
+                sg.check(L.gpu_kin_advance(C.byref(launch), C.byref(ms)), "advance")
+                sg.check(L.gpu_copy_to_host(z.data.ctypes.data, base, z.mutable_rows * z.padded * 8), "down")
+                ref_wall += time.perf_counter() - w0
+                sg.dbd_commit_pulses(z)
+                t = t + SWEEP_DT
+            L.gpu_host_unregister(z.data.ctypes.data)
+            same = got[: z.rows].tobytes() == z.block.tobytes()
+            sim = nsteps * SWEEP_DT
+            results[f"{mode}_{pname}"] = {
+                "steps": nsteps, "sim_s": sim,
+                "device_resident": {"sim_s_per_wall_s": sim / wall_dev, "device_ms_per_step": float(np.mean(dev_ms))},
+                "per_step_upload": {"sim_s_per_wall_s": sim / ref_wall,
+                                    "note": "upload + advance + download per step; host source and commit not timed"},
+                "same_bits": bool(same)}
+            mod.reset_arena()
+    clk = clocks.stop()
+    # the reference's own threaded CPU sweep on the host cores (f32 lanes, its default), bounded
+    cpu = None
+    if not args.no_cpu:
+        from oracle import oracle as O
+
+        if O.ref_available():
+            threads = os.cpu_count() or 1
+            cpu = {"cores": threads, "kind": "reference", "unit": "sim-s per wall-s"}
+            for mode, nsteps in (("pulsed", 1), ("averaged", 5)):
+                z = sweep_zones()
+                blk = sg.dbd_block(z)
+                w0 = time.perf_counter()
+                O.ref_dbd_run(blk, z.cells, z.padded, mode == "pulsed", nsteps, SWEEP_DT,
+                              O.control(rtol=1e-3, atol=1e8, h_min=1e-14, h_start=1e-9, max_steps=20000),
+                              threads=threads, f32_lanes=True)
+                cpu[mode] = nsteps * SWEEP_DT / (time.perf_counter() - w0)
+            cpu["value"] = cpu["pulsed"]
+            cpu["sample"] = ("the reference's dbd_zones_prepare_source + dbd_advance_threads (f32x8 lanes) + "
+                             "commit_pulses on all host threads; 1 pulsed and 5 averaged 20 ms steps of the sweep")
+    head = results["pulsed_f32"]
+    line = {"metric": "sim-s per wall-s (4,096-zone DBD sweep, pulsed)", "value": head["device_resident"]["sim_s_per_wall_s"],
+            "unit": "sim-s/wall-s", "n_gpus": 1, "steps": steps_for["pulsed"], "warmup": 1,
+            "ms_per_step": head["device_resident"]["device_ms_per_step"], "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": head["device_resident"]["sim_s_per_wall_s"] / SWEEP_PULSED_PUBLISHED_CUDA,
+            "vs_baseline_note": "value / 0.09 sim-s per wall-s, the reference's published CUDA pulsed sweep (RTX 3060, "
+                                "f32 lanes, docs/M2_KINETICS.md:203)",
+            "dtype": "f32 lanes (f32 Delta formulation over f64 state)", "data": "synthetic",
+            "config": {"workload": "DBD sweep, 64 x 64 zones (power 0.01-0.5 W/cm^3 x H2O 0-4 %), 310 K, 10 kHz, "
+                                   "20 ms chemistry steps, rtol 1e-3 atol 1e8", "zones": SWEEP_SIDE * SWEEP_SIDE},
+            "modes": results, "cpu_baseline": cpu,
+            "e2e": {"value": head["per_step_upload"]["sim_s_per_wall_s"], "unit": "sim-s/wall-s",
+                    "path": "the reference's dbd_advance_gpu pattern through the C ABI",
+                    "h2d_bytes_per_step": int(sweep_zones().nbytes), "d2h_bytes_per_step": 22 * 4096 * 8},
+            "clocks": clk}
+    print(json.dumps(line))
+
+
 def run_large_mechanism(args):
     """Large synthetic mechanism through the cooperative kernels: mixed on --cells cells (default 65,536),
     FP64 (bit-identical to the reference's algorithm) on the first --fp64-cells of them."""
@@ -892,6 +1019,8 @@ if __name__ == "__main__":
         run_serving(a)
     elif a.workload == "mech200-65536x10s" and a.impl == "ours":
         run_large_mechanism(a)
+    elif a.workload == "dbd-sweep-4096" and a.impl == "ours":
+        run_dbd_sweep(a)
     else:
         if a.workload == "air-4096x1s":   # the reference's CPU-runnable case: 4,096 cells x 1 s
             a.cells = 4096 if a.cells == (1 << 20) else a.cells

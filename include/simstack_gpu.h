@@ -281,13 +281,59 @@ SGB_API void *gpu_stream(void);
  * next call clears the flag). Set-up, once per device with that device
  * current and before any stream capture: the first call looks up the array's
  * device address, and the context's per-thread stack reservation must cover
- * the kernel's frame (gpu_init sets it; without gpu_init, call
- * gpu_stack_limit(3840, ...) -- a call whose kernel needs more returns
- * cudaErrorLaunchOutOfResources instead of letting the driver grow it). Every
+ * the kernel's frame (gpu_init sets 3,840 bytes, which covers the generated
+ * kernels of the shipped mechanism; the table-driven kernels of any other
+ * mechanism need up to 10,752; without gpu_init, call gpu_stack_limit) -- a
+ * call whose kernel needs more returns cudaErrorLaunchOutOfResources instead
+ * of letting the driver grow it. Every
  * call shares the array and clears what must start at zero; calls that
  * overlap on the GPU (other streams, other host threads) race on it. */
 SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *method, const KinControl *control,
                                         const GpuKinLaunch *launch, void *stream, int32_t wait);
+
+/* ---------------------------------------------------------------------------
+ * The DBD zone driver on the device: src/sim/dbd.cpp:118-158 (dbd_zones_prepare_source,
+ * dbd_zones_commit_pulses) and 466-483 (dbd_flow_exchange) as kernels on the module stream,
+ * with the same bits as the reference's host driver. The zone block is the reference's
+ * DbdZones block (dbd.cpp:40-83) mirrored in device memory, host-only rows included, so a
+ * multi-step run keeps it device-resident and uploads nothing between master steps (the
+ * reference uploads the whole block before every advance, dbd.cpp:279). Rate constants and
+ * the source's temperature factors stay host-computed (libm): upload them when T or p change,
+ * as dbd_zones_prepare_rates is called. Shipped humid-air mechanism only (17 species).
+ */
+typedef struct GpuDbdZones {
+    double *y, *h, *steps, *rejects, *pulses, *failed;            /* the solver's rows */
+    double *k, *src, *pulse, *period, *pulse_first, *pulse_count;
+    double *pulse_index, *T_K, *p_Pa, *x_H2O, *power_W_cm3, *freq_Hz; /* DbdZones' host rows, on the device */
+    double *source_temp;   /* [5][padded] temperature factors (kin_air_source_temperature) */
+    uint32_t count, padded, n_species, n_reactions;
+} GpuDbdZones;
+
+/* AirSourceModel (src/sim/kinetics/air_mech.cpp:133-148) with its G-values resolved (per 100
+ * eV at the reference gas's mole fractions; for the Boltzmann option pass the table's values
+ * at the reduced field); filament_J_cm3 > 0 selects the filament pulse rate. NULL = defaults. */
+typedef struct GpuAirSource {
+    double g_O2_diss, f_O1D, g_N2A, g_N2_diss, g_OH_per_100eV, filament_J_cm3;
+} GpuAirSource;
+
+/* Host: the source's five temperature factors per zone, (T/300)^0.55 and exp(c/T) for c = 110,
+ * 55, 60, 20 (air_mech.cpp:230, 265-270), into a [5][padded] block. */
+SGB_API void kin_air_source_temperature(const double *T_K, uint32_t count, uint32_t padded, double *tf);
+/* dbd.cpp:123-152: this master step's source (averaged: per second; pulsed: per pulse) and the
+ * f64 pulse schedule in local time, for every padded zone. Waits. */
+SGB_API int32_t gpu_dbd_prepare_source(const GpuDbdZones *zones, const GpuAirSource *source, uint32_t pulsed, double t0,
+                                       double t1);
+/* dbd.cpp:156-158: pulse_index += pulse_count. Waits. */
+SGB_API int32_t gpu_dbd_commit_pulses(const GpuDbdZones *zones);
+/* dbd.cpp:468-483: explicit upwind plug flow along zones [0, count), zone 0 fed by humid air at
+ * its operating point; cudaErrorInvalidValue when dt count / residence_s > 1. Waits. */
+SGB_API int32_t gpu_dbd_flow_exchange(const GpuDbdZones *zones, double residence_s, double dt);
+/* One master step [t0, t0 + dt] as dbd_scene_step runs it (src/sim/dbd_scene.cpp:226-266): source,
+ * advance of every padded lane over dt (gpu_kin_advance's kernel and tuning), pulse commit, and
+ * the plug flow when `chained`; all on the module stream, nothing copied. Waits; step_ms =
+ * device time of the whole step. */
+SGB_API int32_t gpu_dbd_step(const GpuDbdZones *zones, const GpuAirSource *source, uint32_t pulsed, double t0, double dt,
+                             uint32_t precision, uint32_t chained, double residence_s, float *step_ms);
 
 /* ---------------------------------------------------------------------------
  * Large mechanisms (new capability; the reference's u16 KinMech tables stop

@@ -1237,6 +1237,205 @@ static void advance_mixed_lane(const Mechanism &m, const Method &me, const Contr
     a.pulses[i] += st.pulses;
 }
 
+// Model of the module's mixed path with DOUBLE-FLOAT STATE AND REFINED STAGES
+// (mixed variant 2), in the GPU kernel's operation order: every per-species
+// quantity -- the state y, f at each stage point, the stage right-hand sides,
+// the stage vectors K, y_new and the error norm -- is a double-float (hi + lo
+// FP32 pair, ~48-bit significand) on the FP32 pipe; -J, the LU of W and the
+// triangular solves are FP32 and serve as the preconditioner of one
+// refinement sweep per stage, whose residual r = b - ghinv x + J x is
+// evaluated in double-float with J x formed reaction by reaction at y (no
+// stored Jacobian); only t, h and the per-step scalars are FP64.
+static inline Df2 df_mul_f(Df2 a, float b) {   // double-float times float
+    float p = a.hi * b;
+    float e = std::fma(a.hi, b, -p);
+    e = std::fma(a.lo, b, e);
+    float s = p + e;
+    return Df2{s, e - (s - p)};
+}
+static inline Df2 df_neg(Df2 a) { return Df2{-a.hi, -a.lo}; }
+static inline Df2 df_abs(Df2 a) { return a.hi < 0.0f || (a.hi == 0.0f && a.lo < 0.0f) ? df_neg(a) : a; }
+static inline bool df_less(Df2 a, Df2 b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+static inline Df2 df_two_sum(float a, float b) {   // exact a + b as a normalised pair
+    float s = a + b;
+    float bb = s - a;
+    float e = (a - (s - bb)) + (b - bb);
+    return Df2{s, e};
+}
+// times a small integer coefficient: exact for +-1, +-2, +-4, else a double-float product
+static inline Df2 df_times_int(Df2 a, int c) {
+    if (c == 1) return a;
+    if (c == -1 || c == 2 || c == -2 || c == 4 || c == -4) return df_scale(a, (float)c);
+    return df_mul(a, Df2{(float)c, 0.0f});
+}
+static inline Df2 df_times_coef(Df2 a, double c) {   // method coefficients a_ij, m_i, e_i
+    if (c == 1.0) return a;
+    if (c == -1.0 || c == 2.0 || c == -2.0 || c == 4.0 || c == -4.0 || c == 0.5 || c == -0.5) return df_scale(a, (float)c);
+    return df_mul(a, df_from(c));
+}
+
+// v = J(y) x, reaction by reaction: d rate_r = sum_p k_r (prod_{q != p} y[q]) x[q_p], each
+// term multiplied out from k_r (which keeps products of large number densities in FP32
+// range), then v[s] += net_{r,s} d rate_r in reaction order (the order of eval_fun_df).
+static void eval_jvp_df(const Mechanism &m, const Df2 *k, const Df2 *y, const float *x, Df2 *v) {
+    for (u32 s = 0; s < m.n(); ++s) v[s] = Df2{0.0f, 0.0f};
+    for (u32 r = 0; r < m.R(); ++r) {
+        const Reaction &rx = m.reactions[r];
+        Df2 drate{0.0f, 0.0f};
+        for (u32 p = 0; p < rx.reactant_count; ++p) {
+            Df2 t = k[r];
+            for (u32 q = 0; q < rx.reactant_count; ++q)
+                if (q != p) t = df_mul(t, y[rx.reactant[q]]);
+            t = df_mul_f(t, x[rx.reactant[p]]);
+            drate = p == 0 ? t : df_add(drate, t);
+        }
+        for (u32 e = 0; e < rx.net_count; ++e) v[rx.net_species[e]] = df_add(v[rx.net_species[e]], df_times_int(drate, rx.net_coef[e]));
+    }
+}
+
+static void integrate_mixed_ir(const Mechanism &m, const Method &me, const Control &ctl, Df2 *y, double &t, double t_end,
+                               double &h, Stats<double> &st, MixedWork &w) {
+    const u32 n = m.n();
+    std::vector<float> yhi(n), x(n), x2(n);
+    std::vector<Df2> Y(n), fy(n), b(n), jv(n), kd((size_t)4 * n), ynew(n);
+    Df2 *K[4] = {kd.data(), kd.data() + n, kd.data() + 2 * n, kd.data() + 3 * n};
+    float *a = w.a.data();
+    const Df2 rtol = df_from(ctl.rtol), atol = df_from(ctl.atol);
+    const double inv_n = 1.0 / (double)n;
+    bool active = t < t_end && !(st.failed > 0.0);
+    bool reject_last = false, reject_more = false;
+    h = h > 0.0 ? h : ctl.h_start;
+    u32 iterations = 0;
+    while (active) {
+        if (++iterations > ctl.max_steps) { st.failed = 1.0; break; }
+        double remaining = t_end - t;
+        double h_cap = remaining;
+        if (ctl.h_max > 0.0) h_cap = vmin(h_cap, ctl.h_max);
+        double h_wanted = vmax(h, ctl.h_min);
+        bool last = h_wanted >= remaining;
+        double hs = last ? remaining : vmin(h_wanted, h_cap);
+        const double ghinv = 1.0 / (hs * me.gamma0), hinv = 1.0 / hs;
+        const Df2 gd = df_from(ghinv);
+
+        eval_fun_df(m, w.kd.data(), w.sd.data(), y, fy.data());
+        for (u32 s = 0; s < n; ++s) yhi[s] = y[s].hi;
+        eval_neg_jac(m, w.k32.data(), yhi.data(), a);
+        factor(m, (float)ghinv, a);
+
+        for (u32 stg = 0; stg < me.stages; ++stg) {
+            u32 packed = stg * (stg - 1) / 2;
+            if (stg > 0 && me.new_f[stg]) {   // stage point Y = y + sum_j a_j K_j; f(y) reused when it is y
+                bool moved = false;
+                for (u32 s = 0; s < n; ++s) Y[s] = y[s];
+                for (u32 j = 0; j < stg; ++j) {
+                    double av = me.a[packed + j];
+                    if (av == 0.0) continue;
+                    moved = true;
+                    for (u32 s = 0; s < n; ++s) Y[s] = df_add(Y[s], df_times_coef(K[j][s], av));
+                }
+                if (moved) eval_fun_df(m, w.kd.data(), w.sd.data(), Y.data(), fy.data());
+                else eval_fun_df(m, w.kd.data(), w.sd.data(), y, fy.data());
+            }
+            for (u32 s = 0; s < n; ++s) b[s] = fy[s];
+            for (u32 j = 0; j < stg; ++j) {
+                double c = me.c[packed + j];
+                if (c == 0.0) continue;
+                const Df2 ch = df_from(c * hinv);
+                for (u32 s = 0; s < n; ++s) b[s] = df_add(b[s], df_mul(ch, K[j][s]));
+            }
+            for (u32 s = 0; s < n; ++s) x[s] = b[s].hi;
+            solve(m, a, x.data());
+            // one refinement sweep: r = b - ghinv x + J x in double-float, x += W32^-1 r
+            eval_jvp_df(m, w.kd.data(), y, x.data(), jv.data());
+            for (u32 s = 0; s < n; ++s) x2[s] = df_add(df_add(b[s], df_neg(df_mul_f(gd, x[s]))), jv[s]).hi;
+            solve(m, a, x2.data());
+            for (u32 s = 0; s < n; ++s) K[stg][s] = df_two_sum(x[s], x2[s]);
+        }
+
+        Df2 err2{0.0f, 0.0f};
+        for (u32 s = 0; s < n; ++s) {
+            Df2 yn = y[s], ye{0.0f, 0.0f};
+            bool first_e = true;
+            for (u32 stg = 0; stg < me.stages; ++stg) {
+                if (me.m[stg] != 0.0) yn = df_add(yn, df_times_coef(K[stg][s], me.m[stg]));
+                if (me.e[stg] != 0.0) {
+                    ye = first_e ? df_times_coef(K[stg][s], me.e[stg]) : df_add(ye, df_times_coef(K[stg][s], me.e[stg]));
+                    first_e = false;
+                }
+            }
+            Df2 ay = df_abs(y[s]), an = df_abs(yn);
+            const Df2 scale = df_add(df_mul(rtol, df_less(ay, an) ? an : ay), atol);
+            const float inv = 1.0f / scale.hi;
+            const float q1 = ye.hi * inv;
+            const float q2 = df_add(ye, df_neg(df_mul_f(scale, q1))).hi * inv;
+            const Df2 q = df_two_sum(q1, q2);
+            err2 = df_add(err2, df_mul(q, q));
+            ynew[s] = yn;
+        }
+        double err = std::sqrt(df_to(err2) * inv_n);
+        if (!finite(err)) err = 1e10;
+        double fac = step_factor(err, me.order);
+        bool ok = err <= 1.0 || hs <= ctl.h_min;
+        if (ctl.fixed_step) { ok = true; fac = 1.0; }
+        if (ok) {
+            for (u32 s = 0; s < n; ++s) {
+                Df2 v = ynew[s];
+                if (ctl.clamp_negative && (v.hi < 0.0f || (v.hi == 0.0f && v.lo < 0.0f))) v = Df2{0.0f, 0.0f};
+                y[s] = v;
+            }
+            t = last ? t_end : t + hs;
+        }
+        double h_acc = hs * fac;
+        h_acc = reject_last ? vmin(h_acc, hs) : h_acc;
+        h_acc = (last && fac >= 1.0) ? vmax(h_acc, h_wanted) : h_acc;
+        double h_rej = reject_more ? hs * 0.1 : vmin(hs * fac, hs);
+        if (ctl.fixed_step) { h_acc = h_wanted; h_rej = h_wanted; }
+        h = ok ? h_acc : h_rej;
+        reject_more = !ok && reject_last;
+        reject_last = !ok;
+        st.steps = st.steps + (ok ? 1.0 : 0.0);
+        st.rejects = st.rejects + (ok ? 0.0 : 1.0);
+        active = t < t_end && !(st.failed > 0.0);
+    }
+}
+
+static void advance_mixed_ir_lane(const Mechanism &m, const Method &me, const Control &ctl, const LaneArrays &a, u32 i,
+                                  double duration, MixedWork &w, std::vector<Df2> &y) {
+    const u32 n = m.n(), R = m.R(), p = a.padded;
+    for (u32 s = 0; s < n; ++s) {
+        y[s] = df_from(a.y[(size_t)s * p + i]);
+        w.sd[s] = df_from(a.src[(size_t)s * p + i]);
+    }
+    for (u32 r = 0; r < R; ++r) {
+        w.kd[r] = df_from(a.k[(size_t)r * p + i]);
+        w.k32[r] = w.kd[r].hi;
+    }
+    double h = a.h[i], per = a.period[i], first = a.pulse_first[i], count = a.pulse_count[i];
+    Stats<double> st = {0.0, 0.0, 0.0, a.failed[i]};
+    double t = 0.0, applied = 0.0;
+    for (;;) {
+        bool pending = applied < count;
+        double next_pulse = std::fma(applied, per, first);
+        double seg_end = pending ? vmin(next_pulse, duration) : duration;
+        integrate_mixed_ir(m, me, ctl, y.data(), t, seg_end, h, st, w);
+        bool alive = !(st.failed > 0.0);
+        bool hit = pending && alive && t >= seg_end;
+        if (hit) {
+            for (u32 s = 0; s < n; ++s) y[s] = df_add(y[s], df_from(a.pulse[(size_t)s * p + i]));
+            applied = applied + 1.0;
+            st.pulses = st.pulses + 1.0;
+            h = ctl.h_start;
+        }
+        if ((t >= duration && applied >= count) || !alive) break;
+    }
+    for (u32 s = 0; s < n; ++s) a.y[(size_t)s * p + i] = df_to(y[s]);
+    a.h[i] = h;
+    a.failed[i] = st.failed;
+    a.steps[i] += st.steps;
+    a.rejects[i] += st.rejects;
+    a.pulses[i] += st.pulses;
+}
+
 static void advance_mixed_range(const Mechanism *m, const Method *me, const Control *ctl, u32 sweeps, u32 variant,
                                 const LaneArrays *a, u32 begin, u32 end, double duration) {
     MixedWork w;
@@ -1244,7 +1443,8 @@ static void advance_mixed_range(const Mechanism *m, const Method *me, const Cont
     std::vector<double> y(m->n());
     std::vector<Df2> yd(m->n());
     for (u32 i = begin; i < end; ++i) {
-        if (variant == 1) advance_mixed_df_lane(*m, *me, *ctl, *a, i, duration, w, yd);
+        if (variant == 2) advance_mixed_ir_lane(*m, *me, *ctl, *a, i, duration, w, yd);
+        else if (variant == 1) advance_mixed_df_lane(*m, *me, *ctl, *a, i, duration, w, yd);
         else advance_mixed_lane(*m, *me, *ctl, sweeps, *a, i, duration, w, y);
     }
 }

@@ -310,6 +310,8 @@ def ref() -> C.CDLL:
         L.ref_robertson.argtypes = [i32, C.POINTER(Control), d, vp, vp]
         L.ref_robertson.restype = i32
         L.ref_air_rate_block.argtypes = [vp, vp, u32, u32, vp]
+        L.ref_dbd_run.argtypes = [vp, u32, u32, i32, u32, d, i32, d, C.POINTER(Control), u32, u32]
+        L.ref_dbd_run.restype = i32
         L.ref_air_advance_threads.argtypes = [i32, C.POINTER(Control), C.POINTER(LaneArrays), u32, u32, d, u32]
         L.ref_air_advance_threads.restype = i32
         _ref = L
@@ -356,6 +358,18 @@ def ref_air_advance_threads(method: str, ctl: Control, block: dict, padded: int,
     rc = ref().ref_air_advance_threads(METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, threads)
     if rc != 0:
         raise RuntimeError(f"ref_air_advance_threads: {rc}")
+
+
+def ref_dbd_run(block: np.ndarray, count: int, padded: int, pulsed: bool, steps: int, dt: float, ctl: Control,
+                chained: bool = False, residence_s: float = 0.0, threads: int = 1, f32_lanes: bool = False) -> None:
+    """`steps` master steps of dt of the reference's own zone driver (prepare_source, f64x4
+    generated advance, commit_pulses, plug flow when chained) on a float64 block in the
+    reference's DbdZones layout, in place."""
+    assert block.dtype == np.float64 and block.flags["C_CONTIGUOUS"]
+    rc = ref().ref_dbd_run(block.ctypes.data, count, padded, 0 if pulsed else 1, steps, dt, int(chained), residence_s,
+                           C.byref(ctl), threads, int(f32_lanes))
+    if rc != 0:
+        raise RuntimeError(f"ref_dbd_run: {rc}")
 
 
 def ref_robertson(method: str, ctl: Control, t_end: float = 40.0):

@@ -175,6 +175,62 @@ REF_API s32 ref_air_advance_threads(s32 method_id, const RefControl *rc, const R
     return 0;
 }
 
+// `steps` master steps of dt of the reference's own zone driver on a DbdZones block in the
+// reference's layout (dbd.cpp:60-83: the solver's rows, then pulse_index, T_K, p_Pa, x_H2O,
+// power_W_cm3, freq_Hz): dbd_zones_prepare_source, dbd_advance_cpu<f64x4, AirGenOps>,
+// dbd_zones_commit_pulses and, when chained, dbd_flow_exchange -- dbd_scene_step's sequence
+// (dbd_scene.cpp:232-265) without the scene around it. mode 0 pulsed, 1 averaged; the advance
+// on `threads` host threads (dbd_advance_threads) when threads > 1, f32x8 Delta lanes when
+// f32_lanes (the sweep scene's default precision), else f64x4 lanes.
+REF_API s32 ref_dbd_run(f64 *block, u32 count, u32 padded, s32 mode, u32 steps, f64 dt, s32 chained, f64 residence_s,
+                        const RefControl *rc, u32 threads, u32 f32_lanes) {
+    KinModel *model = air_model();
+    if (padded % 8) return -1;
+    KinMethod method = kin_method(KinMethod_Rodas3);
+    KinControl ctl = to_control(rc);
+    AirSourceModel source = air_source_defaults();
+    DbdZones z = {};
+    z.count = count;
+    z.padded = padded;
+    z.n_species = model->mech.species_count;
+    z.n_reactions = model->mech.reaction_count;
+    u64 p = padded, ns = z.n_species, nr = z.n_reactions;
+    f64 **rows[] = {&z.y, &z.h, &z.steps, &z.rejects, &z.pulses, &z.failed, &z.k, &z.src, &z.pulse, &z.period,
+                    &z.pulse_first, &z.pulse_count, &z.pulse_index, &z.T_K, &z.p_Pa, &z.x_H2O, &z.power_W_cm3, &z.freq_Hz};
+    u64 counts[] = {ns * p, p, p, p, p, p, nr * p, ns * p, ns * p, p, p, p, p, p, p, p, p, p};
+    u64 off = 0;
+    for (u32 i = 0; i < 18; ++i) {
+        *rows[i] = block + off;
+        off += counts[i];
+    }
+    z.block = block;
+    z.block_count = off;
+    f64 t = 0.0;   // the scene clock: t1 = t + dt, then t = t1 (dbd_scene.cpp:232, 266)
+    for (u32 s = 0; s < steps; ++s) {
+        f64 t0 = t, t1 = t + dt;
+        dbd_zones_prepare_source(&z, &g_air_sp, &source, (DbdDischargeMode)mode, t0, t1);
+        if (threads > 1) {   // the sim's own threaded advance (dbd_scene.cpp:261)
+            PlatformAPI api = {};
+            api.add_work_entry = ref_add_work_entry;
+            api.complete_all_work = ref_complete_all_work;
+            PlatformWorkQueue queue;
+            queue.threads = threads;
+            static u8 frame_memory[1 << 20];
+            Arena frame = arena_make(frame_memory, sizeof(frame_memory));
+            dbd_advance_threads(&z, &model->mech, &method, &ctl, dt, 1, f32_lanes ? DbdPrecision_F32 : DbdPrecision_F64, &api,
+                                &queue, threads, &frame);
+        } else if (f32_lanes) {
+            dbd_advance_cpu<f32x8, AirGenOps, true>(&z, &model->mech, &method, &ctl, dt);
+        } else {
+            dbd_advance_cpu<f64x4, AirGenOps>(&z, &model->mech, &method, &ctl, dt);
+        }
+        dbd_zones_commit_pulses(&z);
+        if (chained) dbd_flow_exchange(&z, &g_air_sp, residence_s, dt);
+        t = t1;
+    }
+    return 0;
+}
+
 // Robertson (test_kinetics.cpp:151-180 set-up): one scalar integration.
 REF_API s32 ref_robertson(s32 method_id, const RefControl *rc, f64 t_end, f64 *y3, f64 *stats4) {
     KinModel *model = (KinModel *)calloc(1, sizeof(KinModel));

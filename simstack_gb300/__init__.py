@@ -117,6 +117,17 @@ REFERENCE_EXPORTS = ("gpu_init", "gpu_error_string", "gpu_alloc", "gpu_arena_use
 _lib = None
 
 
+class GpuDbdZones(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("y", "h", "steps", "rejects", "pulses", "failed", "k", "src", "pulse", "period",
+                                          "pulse_first", "pulse_count", "pulse_index", "T_K", "p_Pa", "x_H2O",
+                                          "power_W_cm3", "freq_Hz", "source_temp")] + \
+               [("count", C.c_uint32), ("padded", C.c_uint32), ("n_species", C.c_uint32), ("n_reactions", C.c_uint32)]
+
+
+class GpuAirSource(C.Structure):
+    _fields_ = [(n, C.c_double) for n in ("g_O2_diss", "f_O1D", "g_N2A", "g_N2_diss", "g_OH_per_100eV", "filament_J_cm3")]
+
+
 class GpuError(RuntimeError):
     def __init__(self, code: int, where: str):
         msg = lib().gpu_error_string(code).decode() if _lib is not None else str(code)
@@ -204,6 +215,11 @@ def lib() -> C.CDLL:
             "kin_model_rate_block": (None, [vp, vp, vp, u32, u32, vp]),
             "kin_method_coefficients": (KinMethod, [u32]),
             "kin_air_source_delta": (None, [vp, u32, d, d, vp]),
+            "kin_air_source_temperature": (None, [vp, u32, u32, vp]),
+            "gpu_dbd_prepare_source": (i32, [C.POINTER(GpuDbdZones), C.POINTER(GpuAirSource), u32, d, d]),
+            "gpu_dbd_commit_pulses": (i32, [C.POINTER(GpuDbdZones)]),
+            "gpu_dbd_flow_exchange": (i32, [C.POINTER(GpuDbdZones), d, d]),
+            "gpu_dbd_step": (i32, [C.POINTER(GpuDbdZones), C.POINTER(GpuAirSource), u32, d, d, u32, u32, d, C.POINTER(f)]),
             "sgb_workload_air": (None, [u64, u64, u32, u32, d, d, d, d, vp, vp, vp, vp]),
             "sgb_workload_air_source": (None, [u64, u64, u32, u32, d, d, vp, vp, vp, vp]),
             "sgb_workload_synthetic_mech": (vp, [u64, u32, u32, d, u32, d, d, vp]),
@@ -645,6 +661,57 @@ def dbd_prepare_source(z: ZoneBlock, pulsed: bool, t0: float, t1: float) -> None
 
 def dbd_commit_pulses(z: ZoneBlock) -> None:
     z.pulse_index += z["pulse_count"]
+
+
+DBD_HOST_ROWS = ("pulse_index", "T_K", "p_Pa", "x_H2O", "power_W_cm3", "freq_Hz")
+
+
+def dbd_block(z: ZoneBlock) -> np.ndarray:
+    """The zones as one float64 block in the reference's DbdZones layout (src/sim/dbd.cpp:60-83):
+    the solver's rows, then pulse_index, T_K, p_Pa, x_H2O, power_W_cm3, freq_Hz, followed by
+    the source's five temperature-factor rows (kin_air_source_temperature)."""
+    P = z.padded
+    extra = np.zeros((len(DBD_HOST_ROWS) + 5, P))
+    for j, v in enumerate((z.pulse_index, z.T, z.p_Pa, z.x_H2O, z.power, z.freq)):
+        extra[j] = v
+    tf = np.zeros((5, P))
+    lib().kin_air_source_temperature(_p(np.ascontiguousarray(z.T)), P, P, _p(tf))
+    extra[len(DBD_HOST_ROWS):] = tf
+    out = aligned_empty((z.rows + extra.shape[0]) * P).reshape(-1, P)   # 256-byte aligned, as the arena's blocks
+    out[: z.rows] = z.block
+    out[z.rows:] = extra
+    return out
+
+
+class DeviceZones:
+    """A zone block kept in device memory for the device zone driver (gpu_dbd_*): uploaded
+    once, stepped in place, downloaded when the caller wants it."""
+
+    def __init__(self, module: "Module", z: ZoneBlock):
+        self.z = z
+        self.host = dbd_block(z)
+        self.base = module.alloc(self.host.nbytes)
+        check(lib().gpu_copy_to_device(self.base, _p(self.host), self.host.nbytes), "gpu_copy_to_device")
+        P, rows = z.padded, z.rows
+        self.g = GpuDbdZones()
+        for name in ROWS_ORDER:
+            setattr(self.g, name, self.base + z.row_offset[name] * P * 8)
+        for j, name in enumerate(DBD_HOST_ROWS):
+            setattr(self.g, name, self.base + (rows + j) * P * 8)
+        self.g.source_temp = self.base + (rows + len(DBD_HOST_ROWS)) * P * 8
+        self.g.count, self.g.padded, self.g.n_species, self.g.n_reactions = z.cells, P, z.n, z.R
+
+    def step(self, t0: float, dt: float, pulsed: bool, precision: int = 0, chained: bool = False,
+             residence_s: float = 0.0, source: GpuAirSource | None = None) -> float:
+        ms = C.c_float()
+        check(lib().gpu_dbd_step(C.byref(self.g), C.byref(source) if source is not None else None, int(pulsed), t0, dt,
+                                 precision, int(chained), residence_s, C.byref(ms)), "gpu_dbd_step")
+        return ms.value
+
+    def download(self) -> np.ndarray:
+        """The whole device block (reference layout) into self.host; returns it."""
+        check(lib().gpu_copy_to_host(_p(self.host), self.base, self.host.nbytes), "gpu_copy_to_host")
+        return self.host
 
 
 SERVE_STATES = ("waiting", "running", "done", "failed", "cancelled")

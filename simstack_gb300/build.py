@@ -77,7 +77,9 @@ def build(force: bool = False, jobs: int | None = None) -> str:
         ("kern_air_p1.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=1", "-c", os.path.join(CSRC, "kern_air.cu")]),
         ("kern_air_p2.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=2", "-c", os.path.join(CSRC, "kern_air.cu")]),
         ("kern_air_p3.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=3", "-c", os.path.join(CSRC, "kern_air.cu")]),
+        ("kern_air_p4.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=4", "-c", os.path.join(CSRC, "kern_air.cu")]),
         ("kern_table_p3.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=3", "-c", os.path.join(CSRC, "kern_table.cu")]),
+        ("kern_table_p4.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=4", "-c", os.path.join(CSRC, "kern_table.cu")]),
         ("kern_table_p0.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=0", "-c", os.path.join(CSRC, "kern_table.cu")]),
         ("kern_table_p1.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=1", "-c", os.path.join(CSRC, "kern_table.cu")]),
         ("kern_table_p2.o", [NVCC, *NV_FLAGS, "-DSGB_PREC=2", "-c", os.path.join(CSRC, "kern_table.cu")]),
@@ -85,6 +87,7 @@ def build(force: bool = False, jobs: int | None = None) -> str:
         ("gpu_module.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "gpu_module.cu")]),
         ("static_scratch.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "static_scratch.cu")]),
         ("serve.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "serve.cu")]),
+        ("dbd_driver.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "dbd_driver.cu")]),
         ("kern_coop.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "kern_coop.cu")]),
         ("coop_build.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "coop_build.cpp")]),
         ("mech.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "mech.cpp")]),

@@ -36,6 +36,12 @@ cudaError_t launch_air_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
 cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
+cudaError_t launch_air_p4(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_air_p4(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t launch_table_p4(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_table_p4(uint32_t, uint32_t, size_t, int *);
+cudaError_t local_air_p4(uint32_t, uint32_t, size_t *);
+cudaError_t local_table_p4(uint32_t, size_t *);
 cudaError_t local_air_p0(uint32_t, uint32_t, size_t *);
 cudaError_t local_air_p1(uint32_t, uint32_t, size_t *);
 cudaError_t local_air_p2(uint32_t, uint32_t, size_t *);
@@ -75,7 +81,9 @@ struct Module {
     GpuKinTuning tuning[3];
     uint32_t ir_sweeps = 1;
     uint32_t wait_polls = kSpinLimit;   // poll limit of the table-staging waits
-    uint32_t mixed_variant = 1;    // precision 2: 0 FP64-residual refinement, 1 double-float state (default)
+    // precision 2: 0 FP64-residual refinement, 1 double-float state, 2 double-float state with
+    // refined stages (default: the variant that tracks the FP64 path to its tolerance)
+    uint32_t mixed_variant = 2;
     uint64_t launches = 0;
     float last_ms = 0.0f;
     cudaStream_t copy_in = nullptr, copy_out = nullptr;   // pipelined advance: upload and download streams
@@ -93,6 +101,8 @@ struct Module {
     CoopMech coop_head;
     double *d_coop_scratch = nullptr;
     uint32_t coop_grid = 0;
+    void *d_dbd_scratch = nullptr;   // zone driver: the y rows before a plug-flow exchange
+    size_t dbd_scratch_bytes = 0;
 };
 Module g;
 constexpr uint32_t kSuspendCap = 1u << 16;       // parked cells per launch
@@ -133,6 +143,9 @@ void fill_args(const GpuKinLaunch *L, DevArgs *A) {
 }
 
 cudaError_t occupancy(uint32_t prec, const GpuKinTuning &t, int *blocks) {
+    if (prec == 2 && g.mixed_variant == 2)
+        return g.generated ? occupancy_air_p4(t.kind, t.variant, t.block, blocks)
+                           : occupancy_table_p4(t.kind, t.block, kTableBytes, blocks);
     if (prec == 2 && g.mixed_variant == 1)
         return g.generated ? occupancy_air_p3(t.kind, t.variant, t.block, blocks)
                            : occupancy_table_p3(t.kind, t.block, kTableBytes, blocks);
@@ -151,6 +164,7 @@ cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A,
 // Local memory per thread the kernel of (precision, tuning) needs.
 cudaError_t local_bytes(uint32_t prec, const GpuKinTuning &t, size_t *bytes) {
     const bool df = prec == 2 && g.mixed_variant == 1;
+    if (prec == 2 && g.mixed_variant == 2) return g.generated ? local_air_p4(t.kind, t.variant, bytes) : local_table_p4(t.kind, bytes);
     if (g.generated) {
         if (df) return local_air_p3(t.kind, t.variant, bytes);
         return prec == 0 ? local_air_p0(t.kind, t.variant, bytes) : prec == 1 ? local_air_p1(t.kind, t.variant, bytes)
@@ -210,6 +224,11 @@ cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A,
         s.grid = resident < needed ? resident : needed;
         e = cudaMemsetAsync(A.cursor, 0, sizeof(uint32_t), stream);
         if (e != cudaSuccess) return e;
+    }
+    if (prec == 2 && g.mixed_variant == 2) {
+        if (g.generated) return launch_air_p4(s, A, stream);
+        s.variant = 0;
+        return launch_table_p4(s, A, stream);
     }
     if (prec == 2 && g.mixed_variant == 1) {
         if (g.generated) return launch_air_p3(s, A, stream);
@@ -299,6 +318,9 @@ SGB_API int32_t gpu_init(uint32_t device_index, uint64_t arena_bytes, GpuInfo *i
         cudaFree(g.arena);
         cudaFree(g.d_tables);
         cudaFree(g.d_cursor);
+        if (g.d_dbd_scratch) cudaFree(g.d_dbd_scratch);
+        g.d_dbd_scratch = nullptr;
+        g.dbd_scratch_bytes = 0;
         g.arena = nullptr;
         g.d_tables = nullptr;
         g.d_cursor = nullptr;
@@ -741,7 +763,7 @@ SGB_API int32_t gpu_kin_parked_cells(uint32_t *count) {
 }
 
 SGB_API int32_t gpu_kin_set_mixed_variant(uint32_t variant) {
-    if (variant > 1) return (int32_t)cudaErrorInvalidValue;
+    if (variant > 2) return (int32_t)cudaErrorInvalidValue;
     g.mixed_variant = variant;
     return 0;
 }
@@ -757,6 +779,49 @@ namespace sgb {
 // Module settings read by the allocation-free advance (which needs no gpu_init).
 uint32_t module_wait_polls() { return g.wait_polls; }
 uint32_t module_ir_sweeps() { return g.ir_sweeps; }
+
+// For the device zone driver (dbd_driver.cu): the advance enqueued on the module stream at
+// the precision's tuning (what gpu_kin_advance runs), bracketed by the module's timing events.
+cudaStream_t module_stream() { return g.stream; }
+cudaError_t module_enqueue_advance(const GpuKinLaunch *L) {
+    cudaError_t e = check_launch(L);
+    if (e != cudaSuccess) return e;
+    DevArgs A;
+    fill_args(L, &A);
+    return launch_advance(L->precision, g.tuning[L->precision], A);
+}
+cudaError_t module_mark_start() {
+    if (!g.ready) return cudaErrorInitializationError;
+    return cudaEventRecord(g.kin_start, g.stream);
+}
+cudaError_t module_finish(float *device_ms) {
+    cudaError_t e = cudaEventRecord(g.kin_stop, g.stream);
+    if (e == cudaSuccess) e = cudaEventSynchronize(g.kin_stop);
+    if (e != cudaSuccess) return e;
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, g.kin_start, g.kin_stop);
+    g.last_ms = ms;
+    ++g.launches;
+    if (device_ms) *device_ms = ms;
+    e = read_error_flag();
+    return e != cudaSuccess ? e : cudaGetLastError();
+}
+// Module-owned scratch of at least `bytes`, grown (after the stream drains) when too small.
+cudaError_t module_scratch(size_t bytes, void **out) {
+    if (!g.ready) return cudaErrorInitializationError;
+    if (g.dbd_scratch_bytes < bytes) {
+        cudaError_t e = cudaStreamSynchronize(g.stream);
+        if (e != cudaSuccess) return e;
+        if (g.d_dbd_scratch) cudaFree(g.d_dbd_scratch);
+        g.d_dbd_scratch = nullptr;
+        g.dbd_scratch_bytes = 0;
+        e = cudaMalloc(&g.d_dbd_scratch, bytes);
+        if (e != cudaSuccess) return e;
+        g.dbd_scratch_bytes = bytes;
+    }
+    *out = g.d_dbd_scratch;
+    return cudaSuccess;
+}
 }   // namespace sgb
 
 // Measured instruction throughput (operations per second over the device):

@@ -1,5 +1,5 @@
 // Straight-line (generated) kernels for the shipped mechanism with Rodas3
-// coefficients folded in; one precision per compilation (-DSGB_PREC=0|1|2|3).
+// coefficients folded in; one precision per compilation (-DSGB_PREC=0|1|2|3|4).
 
 #include "kin_kernels.cuh"
 
@@ -8,7 +8,7 @@ namespace sgb {
 }
 
 #ifndef SGB_PREC
-#error "compile with -DSGB_PREC=0, 1, 2 or 3"
+#error "compile with -DSGB_PREC=0, 1, 2, 3 or 4"
 #endif
 
 #define SGB_CAT2(a, b) a##b

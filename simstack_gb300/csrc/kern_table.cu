@@ -1,13 +1,13 @@
 // Table-driven kernels (any mechanism within the KinMech capacities, any
 // method of up to four stages), one precision per compilation
-// (-DSGB_PREC=0|1|2|3). A single register-budget variant: the per-lane arrays of
+// (-DSGB_PREC=0|1|2|3|4). A single register-budget variant: the per-lane arrays of
 // the generic path live in local memory whatever the budget.
 
 #include "kin_kernels.cuh"
 #include "kin_table.cuh"
 
 #ifndef SGB_PREC
-#error "compile with -DSGB_PREC=0, 1, 2 or 3"
+#error "compile with -DSGB_PREC=0, 1, 2, 3 or 4"
 #endif
 
 #define SGB_CAT2(a, b) a##b

@@ -82,6 +82,35 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
     for (uint32_t s = 0; s < n; ++s) fprintf(f, "        fhi[%u] = acc[%u].hi; flo[%u] = acc[%u].lo;\n", s, s, s, s);
     fprintf(f, "    }\n\n");
 
+    // mixed variant 2: v = J(y) x in double-float, reaction by reaction: d rate_r = sum_p
+    // k_r (prod_{q != p} y_q) x_p with every term multiplied out from k_r (keeps products of
+    // large number densities in FP32 range), then v_s += net_{r,s} d rate_r in reaction order
+    fprintf(f, "    static __device__ __forceinline__ void jvp_df(const float *__restrict__ khi, const float *__restrict__ klo, const float *__restrict__ yhi, const float *__restrict__ ylo, const float *__restrict__ x, float *__restrict__ vhi, float *__restrict__ vlo) {\n");
+    fprintf(f, "        Df acc[%u];\n", n);
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        acc[%u] = Df{0.0f, 0.0f};\n", s);
+    for (uint32_t r = 0; r < R; ++r) {
+        const Reaction &rx = m.reactions[r];
+        if (rx.reactants.empty()) continue;
+        fprintf(f, "        { Df drate;\n");
+        for (size_t p = 0; p < rx.reactants.size(); ++p) {
+            fprintf(f, "          { Df t = Df{khi[%u], klo[%u]};", r, r);
+            for (size_t q = 0; q < rx.reactants.size(); ++q)
+                if (q != p) fprintf(f, " t = df_mul(t, Df{yhi[%u], ylo[%u]});", rx.reactants[q], rx.reactants[q]);
+            fprintf(f, " t = df_mul_f(t, x[%u]);", rx.reactants[p]);
+            fprintf(f, p == 0 ? " drate = t; }\n" : " drate = df_add(drate, t); }\n");
+        }
+        for (auto &e : rx.net) {
+            int c = e.second;
+            if (c == 1) fprintf(f, "          acc[%u] = df_add(acc[%u], drate);\n", e.first, e.first);
+            else if (c == -1 || c == 2 || c == -2 || c == 4 || c == -4)
+                fprintf(f, "          acc[%u] = df_add(acc[%u], df_scale(drate, %d.0f));\n", e.first, e.first, c);
+            else fprintf(f, "          acc[%u] = df_add(acc[%u], df_mul(drate, Df{%d.0f, 0.0f}));\n", e.first, e.first, c);
+        }
+        fprintf(f, "        }\n");
+    }
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        vhi[%u] = acc[%u].hi; vlo[%u] = acc[%u].lo;\n", s, s, s, s);
+    fprintf(f, "    }\n\n");
+
     // mixed path: FP32 RHS increment f(y + d) - f(y) from the exact expansion
     // prod(y_q + d_q) - prod(y_q) = sum_p k d_p prod_{q<p} y_q prod_{q>p} (y_q + d_q)
     fprintf(f, "    static __device__ __forceinline__ void fun_delta(const float *__restrict__ k, const float *__restrict__ y, const float *__restrict__ d, float *__restrict__ df) {\n");

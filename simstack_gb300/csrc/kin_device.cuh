@@ -897,6 +897,313 @@ struct LaneDf {
 
 
 // ---------------------------------------------------------------------------
+// Mixed path, double-float state with refined stages (mixed variant 2): every
+// per-species quantity -- y, f at each stage point, the stage right-hand sides
+// b, the stage vectors K, y_new and the error norm -- is a double-float on the
+// FP32 pipe; -J, the LU of W and the triangular solves are FP32 and precondition
+// one refinement sweep per stage, whose residual r = b - ghinv x + J x is formed
+// in double-float with J x evaluated reaction by reaction at y (no stored
+// Jacobian). Only t, h and a few scalars per step are FP64. Its results track
+// the FP64 path to ~1e-8 (config-1 inputs, 1 s) where an FP32 solve alone
+// leaves ~1e-3 on species near atol.
+
+__device__ __forceinline__ Df df_mul_f(Df a, float b) {   // double-float times float
+    const float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    const float s = p + e;
+    return Df{s, e - (s - p)};
+}
+__device__ __forceinline__ Df df_neg(Df a) { return Df{-a.hi, -a.lo}; }
+__device__ __forceinline__ Df df_abs(Df a) { return a.hi < 0.0f || (a.hi == 0.0f && a.lo < 0.0f) ? df_neg(a) : a; }
+__device__ __forceinline__ bool df_less(Df a, Df b) { return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo); }
+__device__ __forceinline__ Df df_two_sum(float a, float b) {   // exact a + b, normalised
+    const float s = a + b;
+    const float bb = s - a;
+    const float e = (a - (s - bb)) + (b - bb);
+    return Df{s, e};
+}
+// times a method coefficient: exact for +-1, +-2, +-4, +-1/2, else a double-float product
+__device__ __forceinline__ Df df_times_coef(Df a, double c) {
+    if (c == 1.0) return a;
+    if (c == -1.0 || c == 2.0 || c == -2.0 || c == 4.0 || c == -4.0 || c == 0.5 || c == -0.5) return df_scale(a, (float)c);
+    return df_mul(a, df_from(c));
+}
+
+template <class Ops, class M>
+struct LaneIr {
+    static constexpr int N = Ops::N, R = Ops::R, NNZ = Ops::NNZ, S = M::kStages;
+    static constexpr size_t kSmemBytes = 0;
+
+    Ops ops;
+    float yhi[N], ylo[N];
+    float khi[R], klo[R], shi[N], slo[N];
+    double t, h, seg_end, applied, duration, period, first, count;
+    double steps, rejects, pulses, failed;
+    uint32_t iterations, transitions, attempts;
+    int phase;
+    bool pending, reject_last, reject_more;
+    float lu[NNZ];
+    float Yhi[N], Ylo[N], fhi[N], flo[N], bhi[N], blo[N], vhi[N], vlo[N];
+    float Khi[S][N], Klo[S][N];
+    float x[N], x2[N];
+
+    __device__ __forceinline__ void bind(unsigned char *) {}
+    __device__ __forceinline__ uint32_t n() const { return ops.n(); }
+
+    __device__ __forceinline__ void load(const DevArgs &A, uint32_t i) {
+        const uint32_t p = A.padded, nn = n(), rr_ = ops.r();
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            Df v = df_from(A.y[(size_t)s * p + i]);
+            yhi[s] = v.hi;
+            ylo[s] = v.lo;
+            v = df_from(A.src[(size_t)s * p + i]);
+            shi[s] = v.hi;
+            slo[s] = v.lo;
+        }
+        for (int r = 0; r < R; ++r) {
+            if (r >= (int)rr_) break;
+            const Df v = df_from(A.k[(size_t)r * p + i]);
+            khi[r] = v.hi;
+            klo[r] = v.lo;
+        }
+        h = A.h[i];
+        period = A.period[i];
+        first = A.pulse_first[i];
+        count = A.pulse_count[i];
+        duration = A.duration;
+        steps = rejects = pulses = 0.0;
+        failed = A.failed[i];
+        t = 0.0;
+        applied = 0.0;
+        transitions = 0;
+        attempts = 0;
+        phase = kPhaseSegStart;
+    }
+
+    __device__ __forceinline__ void store(const DevArgs &A, uint32_t i) {
+        const uint32_t p = A.padded, nn = n();
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            A.y[(size_t)s * p + i] = df_to(Df{yhi[s], ylo[s]});
+        }
+        A.h[i] = h;
+        A.failed[i] = failed;
+        A.steps[i] += steps;
+        A.rejects[i] += rejects;
+        A.pulses[i] += pulses;
+    }
+
+    __device__ __forceinline__ void seg_start(const DevArgs &A) {
+        pending = applied < count;
+        double next_pulse = sgb_fma(applied, period, first);
+        seg_end = pending ? vmin(next_pulse, duration) : duration;
+        bool active = t < seg_end && !(failed > 0.0);
+        reject_last = false;
+        reject_more = false;
+        h = h > 0.0 ? h : A.ctl.h_start;
+        iterations = 0;
+        phase = active ? kPhaseStepping : kPhaseSegFinish;
+    }
+
+    __device__ __forceinline__ void seg_finish(const DevArgs &A, uint32_t cell) {
+        bool alive = !(failed > 0.0);
+        bool hit = pending && alive && t >= seg_end;
+        if (hit) {
+            const uint32_t p = A.padded, nn = n();
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                const Df v = df_add(Df{yhi[s], ylo[s]}, df_from(A.pulse[(size_t)s * p + cell]));
+                yhi[s] = v.hi;
+                ylo[s] = v.lo;
+            }
+            applied = applied + 1.0;
+            pulses = pulses + 1.0;
+            h = A.ctl.h_start;
+        }
+        bool done = (t >= duration && applied >= count) || !alive;
+        phase = done ? kPhaseDone : kPhaseSegStart;
+    }
+
+    __device__ __forceinline__ bool settle(const DevArgs &A, uint32_t) {
+        for (;;) {
+            if (++transitions > (1u << 24)) {
+                failed = 1.0;
+                phase = kPhaseDone;
+            }
+            switch (phase) {
+                case kPhaseSegStart: seg_start(A); break;
+                case kPhaseSegFinish: seg_finish(A, 0); break;
+                case kPhaseStepping:
+                    ++attempts;
+                    if (++iterations > A.ctl.max_steps) {
+                        failed = 1.0;
+                        phase = kPhaseSegFinish;
+                        break;
+                    }
+                    return true;
+                default: return false;
+            }
+        }
+    }
+
+    template <bool kSync = false>
+    __device__ __forceinline__ void attempt(const DevArgs &A, bool commit = true) {
+        const uint32_t nn = n();
+        const double remaining = seg_end - t;
+        double h_cap = remaining;
+        if (A.ctl.h_max > 0.0) h_cap = vmin(h_cap, A.ctl.h_max);
+        const double h_wanted = vmax(h, A.ctl.h_min);
+        const bool last = h_wanted >= remaining;
+        const double hs = last ? remaining : vmin(h_wanted, h_cap);
+        const double ghinv = 1.0 / (hs * M::gamma0(A)), hinv = 1.0 / hs;
+        const Df gd = df_from(ghinv);
+
+        ops.neg_jac(khi, yhi, lu);   // FP32 -J at the FP32 rounding of y
+        if constexpr (kSync) __syncthreads();
+        ops.factor((float)ghinv, lu);
+        if constexpr (kSync) __syncthreads();
+
+        bool f_at_y = false;   // f (fhi, flo) holds f(y)
+#pragma unroll 1
+        for (int st = 0; st < S; ++st) {
+            if (st >= M::stages(A)) break;
+            const int packed = st * (st - 1) / 2;
+            if (st == 0 || M::new_f(A, st)) {
+                // stage point Y = y + sum_j a_j K_j; f(y) is reused when the point is y
+                bool moved = false;
+                for (int s = 0; s < N; ++s) {
+                    if (s >= (int)nn) break;
+                    Yhi[s] = yhi[s];
+                    Ylo[s] = ylo[s];
+                }
+#pragma unroll
+                for (int j = 0; j < S - 1; ++j) {
+                    if (j >= st) break;
+                    const double a = M::a(A, packed + j);
+                    if (a == 0.0) continue;
+                    moved = true;
+                    for (int s = 0; s < N; ++s) {
+                        if (s >= (int)nn) break;
+                        const Df v = df_add(Df{Yhi[s], Ylo[s]}, df_times_coef(Df{Khi[j][s], Klo[j][s]}, a));
+                        Yhi[s] = v.hi;
+                        Ylo[s] = v.lo;
+                    }
+                }
+                if (moved || !f_at_y) {
+                    ops.fun_df(khi, klo, shi, slo, Yhi, Ylo, fhi, flo);
+                    f_at_y = !moved;
+                }
+            }
+            // b = f + sum_j (c_j / h) K_j in double-float
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                bhi[s] = fhi[s];
+                blo[s] = flo[s];
+            }
+#pragma unroll
+            for (int j = 0; j < S - 1; ++j) {
+                if (j >= st) break;
+                const double c = M::c(A, packed + j);
+                if (c == 0.0) continue;
+                const Df ch = df_from(c * hinv);
+                for (int s = 0; s < N; ++s) {
+                    if (s >= (int)nn) break;
+                    const Df v = df_add(Df{bhi[s], blo[s]}, df_mul(ch, Df{Khi[j][s], Klo[j][s]}));
+                    bhi[s] = v.hi;
+                    blo[s] = v.lo;
+                }
+            }
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                x[s] = bhi[s];
+            }
+            ops.solve(lu, x);
+            // one refinement sweep: r = b - ghinv x + J x (double-float), x2 = W32^-1 r
+            ops.jvp_df(khi, klo, yhi, ylo, x, vhi, vlo);
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                x2[s] = df_add(df_add(Df{bhi[s], blo[s]}, df_neg(df_mul_f(gd, x[s]))), Df{vhi[s], vlo[s]}).hi;
+            }
+            ops.solve(lu, x2);
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                const Df v = df_two_sum(x[s], x2[s]);
+                Khi[st][s] = v.hi;
+                Klo[st][s] = v.lo;
+            }
+            if constexpr (kSync) __syncthreads();
+        }
+
+        // y_new and the weighted RMS error, both in double-float
+        const Df rtol = df_from(A.ctl.rtol), atol = df_from(A.ctl.atol);
+        Df err2{0.0f, 0.0f};
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            Df yn{yhi[s], ylo[s]}, ye{0.0f, 0.0f};
+            bool first_e = true;
+#pragma unroll
+            for (int st = 0; st < S; ++st) {
+                if (st >= M::stages(A)) break;
+                const double mc = M::m(A, st), ec = M::e(A, st);
+                const Df kv{Khi[st][s], Klo[st][s]};
+                if (mc != 0.0) yn = df_add(yn, df_times_coef(kv, mc));
+                if (ec != 0.0) {
+                    ye = first_e ? df_times_coef(kv, ec) : df_add(ye, df_times_coef(kv, ec));
+                    first_e = false;
+                }
+            }
+            const Df ay = df_abs(Df{yhi[s], ylo[s]}), an = df_abs(yn);
+            const Df scale = df_add(df_mul(rtol, df_less(ay, an) ? an : ay), atol);
+            const float inv = 1.0f / scale.hi;
+            const float q1 = ye.hi * inv;
+            const float q2 = df_add(ye, df_neg(df_mul_f(scale, q1))).hi * inv;
+            const Df q = df_two_sum(q1, q2);
+            err2 = df_add(err2, df_mul(q, q));
+            Yhi[s] = yn.hi;   // y_new, kept in the stage-point buffer
+            Ylo[s] = yn.lo;
+        }
+        double err = sqrt(df_to(err2) * (1.0 / (double)nn));
+        if (!is_finite_lane(err)) err = 1e10;
+        double fac = step_factor(err, M::order(A));
+        bool ok = err <= 1.0 || hs <= A.ctl.h_min;
+        if (A.ctl.fixed_step) {
+            ok = true;
+            fac = 1.0;
+        }
+        if (!commit) return;
+        if (ok) {
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                float hi = Yhi[s], lo = Ylo[s];
+                if (A.ctl.clamp_negative && (hi < 0.0f || (hi == 0.0f && lo < 0.0f))) {
+                    hi = 0.0f;
+                    lo = 0.0f;
+                }
+                yhi[s] = hi;
+                ylo[s] = lo;
+            }
+            t = last ? seg_end : t + hs;
+        }
+        double h_acc = hs * fac;
+        h_acc = reject_last ? vmin(h_acc, hs) : h_acc;
+        h_acc = (last && fac >= 1.0) ? vmax(h_acc, h_wanted) : h_acc;
+        double h_rej = reject_more ? hs * 0.1 : vmin(hs * fac, hs);
+        if (A.ctl.fixed_step) {
+            h_acc = h_wanted;
+            h_rej = h_wanted;
+        }
+        h = ok ? h_acc : h_rej;
+        reject_more = !ok && reject_last;
+        reject_last = !ok;
+        steps = steps + (ok ? 1.0 : 0.0);
+        rejects = rejects + (ok ? 0.0 : 1.0);
+        if (!(t < seg_end && !(failed > 0.0))) phase = kPhaseSegFinish;
+    }
+};
+
+// ---------------------------------------------------------------------------
 // Generated straight-line ops (kin_codegen.cpp) as an Ops object.
 
 // SGB_OPS_QUALIFIER: __forceinline__ (default) inlines every op at every call
@@ -927,6 +1234,10 @@ struct GenOps {
         G::fun_df(khi, klo, shi, slo, yhi, ylo, fhi, flo);
     }
     __device__ SGB_OPS_QUALIFIER void fun_delta(const float *k, const float *y, const float *d, float *df) const { G::fun_delta(k, y, d, df); }
+    __device__ SGB_OPS_QUALIFIER void jvp_df(const float *khi, const float *klo, const float *yhi, const float *ylo, const float *x,
+                                             float *vhi, float *vlo) const {
+        G::jvp_df(khi, klo, yhi, ylo, x, vhi, vlo);
+    }
     __device__ SGB_OPS_QUALIFIER void save_jac(const float *a, double *js) const { G::save_jac(a, js); }
     __device__ SGB_OPS_QUALIFIER void residual(const double *js, double ghinv, const double *b, const double *x, double *r) const {
         G::residual(js, ghinv, b, x, r);

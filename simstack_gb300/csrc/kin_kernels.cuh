@@ -32,12 +32,14 @@ template <> struct Budget<3> { static constexpr int kThreads = 512, kMinBlocks =
 #endif
 
 // The lane type of a precision: 0 FP64, 1 f32 Delta, 2 mixed with FP64
-// refinement, 3 mixed with double-float state.
+// refinement, 3 mixed with double-float state, 4 mixed with double-float state
+// and refined stages.
 template <class Ops, class M, int PREC, int V> struct LaneOf { typedef Lane<Ops, M, PREC> type; };
 template <class Ops, class M, int V> struct LaneOf<Ops, M, 3, V> {
     static constexpr int kStride = (SGB_SHARED_LU && Ops::kStridedLu && Budget<V>::kThreads <= 256) ? Budget<V>::kThreads : 0;
     typedef LaneDf<Ops, M, kStride> type;
 };
+template <class Ops, class M, int V> struct LaneOf<Ops, M, 4, V> { typedef LaneIr<Ops, M> type; };
 
 // Both kernels keep every lane of a warp in the loop until the whole warp is
 // out of work, and vote (__any_sync) once per iteration: the vote is a

@@ -135,6 +135,38 @@ struct TableOps {
         }
     }
 
+    // v = J(y) x in double-float in the generated code's order (kin_codegen.cpp, jvp_df).
+    __device__ __forceinline__ void jvp_df(const float *khi, const float *klo, const float *yhi, const float *ylo, const float *x,
+                                           float *vhi, float *vlo) const {
+        const uint32_t ns = m->species_count, nr = m->reaction_count;
+        for (uint32_t s = 0; s < ns; ++s) {
+            vhi[s] = 0.0f;
+            vlo[s] = 0.0f;
+        }
+        for (uint32_t r = 0; r < nr; ++r) {
+            const KinReaction &rx = m->reactions[r];
+            if (rx.reactant_count == 0) continue;
+            Df drate{0.0f, 0.0f};
+            for (uint32_t p = 0; p < rx.reactant_count; ++p) {
+                Df t{khi[r], klo[r]};
+                for (uint32_t q = 0; q < rx.reactant_count; ++q)
+                    if (q != p) t = df_mul(t, Df{yhi[rx.reactant[q]], ylo[rx.reactant[q]]});
+                t = df_mul_f(t, x[rx.reactant[p]]);
+                drate = p == 0 ? t : df_add(drate, t);
+            }
+            for (uint32_t e = 0; e < rx.net_count; ++e) {
+                const uint32_t s = rx.net_species[e];
+                const int c = rx.net_coef[e];
+                Df term = c == 1 ? drate
+                          : (c == -1 || c == 2 || c == -2 || c == 4 || c == -4) ? df_scale(drate, (float)c)
+                                                                                 : df_mul(drate, Df{(float)c, 0.0f});
+                const Df acc = df_add(Df{vhi[s], vlo[s]}, term);
+                vhi[s] = acc.hi;
+                vlo[s] = acc.lo;
+            }
+        }
+    }
+
     __device__ __forceinline__ bool in_jac(uint32_t slot) const {
         const uint8_t *mask = (const uint8_t *)m + kJacMaskOffset;
         return (mask[slot >> 3] >> (slot & 7)) & 1u;

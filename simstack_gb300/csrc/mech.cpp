@@ -3,6 +3,7 @@
 // bits must match the reference's kin_eval_rate_constants.
 
 #include "mech.h"
+#include "air_source.h"
 
 #include <math.h>
 #include <string.h>
@@ -344,97 +345,21 @@ KinMethod method_coefficients(uint32_t id) {
 }
 
 // ---------------------------------------------------------------------------
-// Averaged / per-pulse discharge source of the shipped mechanism
-// (air_mech.cpp:164-276, default G-values): electron-impact channels, then the
-// quasi-steady fates of N2(A), N(2D) and O(1D), each distributed over its
-// partners in proportion to k [partner] with a half-partner cap.
+// Averaged / per-pulse discharge source (air_mech.cpp:164-276, default G-values): the
+// shared restatement of air_source.h with the temperature factors from host libm.
 
-namespace {
-enum : uint32_t { O = 0, O3, N, NO, NO2, NO3, N2O5, N2O, HNO2, HNO3, OH, HO2, H2O2, H, N2, O2, H2O };
-struct Fate { double k; uint32_t partner; };
-
-void split_fates(const Fate *fate, uint32_t count, const double *y, double amount, double *share) {
-    double sum = 0.0;
-    uint32_t big = 0;
-    for (uint32_t c = 0; c < count; ++c) {
-        share[c] = fate[c].k * y[fate[c].partner];
-        if (share[c] > share[big]) big = c;
-        sum += share[c];
-    }
-    if (sum <= 0.0) {
-        for (uint32_t c = 0; c < count; ++c) share[c] = c == big ? 1.0 : 0.0;
-        return;
-    }
-    double moved = 0.0;
-    for (uint32_t c = 0; c < count; ++c) {
-        share[c] /= sum;
-        double cap = amount > 0.0 ? 0.5 * y[fate[c].partner] / amount : 1.0;
-        if (c != big && share[c] > cap) {
-            moved += share[c] - cap;
-            share[c] = cap;
-        }
-    }
-    share[big] += moved;
+void air_source_temperature(double T_K, double *tf) {
+    tf[0] = pow(T_K / 300.0, 0.55);
+    tf[1] = exp(110.0 / T_K);
+    tf[2] = exp(55.0 / T_K);
+    tf[3] = exp(60.0 / T_K);
+    tf[4] = exp(20.0 / T_K);
 }
-}   // namespace
 
 void air_source_delta(const double *y, uint32_t n, double energy_J_cm3, double T_K, double *d) {
-    for (uint32_t s = 0; s < n; ++s) d[s] = 0.0;
-    double total = 0.0;
-    for (uint32_t s = 0; s < n; ++s) total += y[s];
-    if (total <= 0.0 || energy_J_cm3 <= 0.0) return;
-    const double g_o2 = 1.5, f_o1d = 0.5, g_n2a = 1.5, g_n2d = 0.4, g_oh = 0.3;
-    double hundreds_eV = energy_J_cm3 * 6.241509074e18 * 0.01;
-    double dO2 = g_o2 * (y[O2] / total / 0.21) * hundreds_eV;
-    double dA = g_n2a * (y[N2] / total / 0.78) * hundreds_eV;
-    double dN2 = g_n2d * (y[N2] / total / 0.78) * hundreds_eV;
-    double dOH = g_oh * (y[H2O] / total / 0.02) * hundreds_eV;
-    double d1D = f_o1d * dO2;
-    d[O2] -= dO2;
-    d[O] += 2.0 * dO2 - d1D;
-    d[N2] -= dA + dN2;
-    d[N] += dN2;
-    d[OH] += dOH;
-    d[H] += dOH;
-    d[H2O] -= dOH;
-    double k_o2 = pow(T_K / 300.0, 0.55);
-    double f[10];
-    const Fate n2a[9] = {{2.5e-12 * k_o2, O2}, {1.3e-12 * k_o2, O2}, {7.8e-14 * k_o2, O2}, {7.0e-12, O}, {7.0e-11, NO},
-                         {1.0e-12, NO2},       {8.0e-11, N2O},       {5.0e-14, H2O},       {3.0e-16, N2}};
-    split_fates(n2a, 9, y, dA, f);
-    d[N2] += dA * (f[0] + f[1] + f[4] + f[5] + f[6] + f[7] + f[8]);
-    d[O2] -= dA * (f[0] + f[2]);
-    d[O] += dA * (2.0 * f[0] + f[2] + f[5]);
-    d[N2O] += dA * (f[2] - f[6]);
-    d[O] -= dA * f[3];
-    d[NO] += dA * (f[3] + f[5] + f[6]);
-    double n2d = dN2 + dA * f[3];
-    d[NO2] -= dA * f[5];
-    d[N] += dA * f[6];
-    d[H2O] -= dA * f[7];
-    d[H] += dA * f[7];
-    d[OH] += dA * f[7];
-    const Fate n2dfate[5] = {{5.2e-12, O2}, {1.7e-14, N2}, {6.9e-13, O}, {6.0e-11, NO}, {2.2e-12, N2O}};
-    split_fates(n2dfate, 5, y, n2d, f);
-    d[O2] -= n2d * f[0];
-    d[NO] += n2d * (f[0] - f[3] + f[4]);
-    d[O] += n2d * (f[0] + f[3]);
-    d[N] += n2d * (f[1] + f[2]);
-    d[N2] += n2d * (f[3] + f[4]);
-    d[N2O] -= n2d * f[4];
-    const Fate o1d[6] = {{2.15e-11 * exp(110.0 / T_K), N2}, {3.3e-11 * exp(55.0 / T_K), O2}, {1.63e-10 * exp(60.0 / T_K), H2O},
-                         {7.26e-11 * exp(20.0 / T_K), N2O}, {4.63e-11 * exp(20.0 / T_K), N2O}, {2.4e-10, O3}};
-    split_fates(o1d, 6, y, d1D, f);
-    d[O] += d1D * (f[0] + f[1]);
-    d[O3] -= d1D * f[5];
-    d[O2] += d1D * f[5] * 1.5;
-    d[O] += d1D * f[5];
-    d[H2O] -= d1D * f[2];
-    d[OH] += d1D * f[2] * 2.0;
-    d[N2O] -= d1D * (f[3] + f[4]);
-    d[NO] += d1D * f[3] * 2.0;
-    d[N2] += d1D * f[4];
-    d[O2] += d1D * f[4];
+    double tf[kAirTempFactors];
+    air_source_temperature(T_K, tf);
+    air_source_delta_tf(y, n, energy_J_cm3, air_source_defaults(), tf, d);
 }
 
 }   // namespace sgb

@@ -90,6 +90,8 @@ void define_air(Model *m);   // the shipped 17-species, 44-reaction humid-air me
 uint64_t fnv1a(const void *data, uint64_t size);
 KinMethod method_coefficients(uint32_t id);
 void air_source_delta(const double *y, uint32_t n, double energy_J_cm3, double T_K, double *delta);
+// The five temperature factors of the source's channel rates (host libm), for air_source_delta_tf.
+void air_source_temperature(double T_K, double *tf);
 
 }   // namespace sgb
 

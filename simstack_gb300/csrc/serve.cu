@@ -60,6 +60,10 @@ cudaError_t launch_air_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
 cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
+cudaError_t launch_air_p4(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_air_p4(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t launch_table_p4(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_table_p4(uint32_t, uint32_t, size_t, int *);
 uint64_t air_ops_signature();
 size_t coop_smem_bytes_for(int prec, const CoopMech &h);
 size_t coop_scratch_doubles_for(int prec, const CoopMech &h);
@@ -187,19 +191,24 @@ Engine E;
 
 uint32_t pad8(uint32_t c) { return (c + 7u) / 8u * 8u; }
 
-// p: 0 FP64, 1 f32 Delta, 2 mixed with FP64 refinement, 3 mixed with double-float state
+// p: 0 FP64, 1 f32 Delta, 2 mixed with FP64 refinement, 3 mixed with double-float state,
+// 4 mixed with double-float state and refined stages
 cudaError_t launch_chem(bool generated, uint32_t p, const Shape &sh, const DevArgs &A, cudaStream_t s) {
     if (generated)
-        return p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : p == 2 ? launch_air_p2(sh, A, s) : launch_air_p3(sh, A, s);
-    return p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : p == 2 ? launch_table_p2(sh, A, s) : launch_table_p3(sh, A, s);
+        return p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : p == 2 ? launch_air_p2(sh, A, s)
+               : p == 3 ? launch_air_p3(sh, A, s) : launch_air_p4(sh, A, s);
+    return p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : p == 2 ? launch_table_p2(sh, A, s)
+           : p == 3 ? launch_table_p3(sh, A, s) : launch_table_p4(sh, A, s);
 }
 
 cudaError_t occupancy_chem(bool generated, uint32_t p, uint32_t block, size_t smem, int *per_sm) {
     if (generated)
         return p == 0 ? occupancy_air_p0(2, 0, block, per_sm) : p == 1 ? occupancy_air_p1(2, 0, block, per_sm)
-               : p == 2 ? occupancy_air_p2(2, 0, block, per_sm) : occupancy_air_p3(2, 0, block, per_sm);
+               : p == 2 ? occupancy_air_p2(2, 0, block, per_sm) : p == 3 ? occupancy_air_p3(2, 0, block, per_sm)
+               : occupancy_air_p4(2, 0, block, per_sm);
     return p == 0 ? occupancy_table_p0(2, block, smem, per_sm) : p == 1 ? occupancy_table_p1(2, block, smem, per_sm)
-           : p == 2 ? occupancy_table_p2(2, block, smem, per_sm) : occupancy_table_p3(2, block, smem, per_sm);
+           : p == 2 ? occupancy_table_p2(2, block, smem, per_sm) : p == 3 ? occupancy_table_p3(2, block, smem, per_sm)
+           : occupancy_table_p4(2, block, smem, per_sm);
 }
 
 // Frees a request's device resources in stream order (no device-wide synchronisation).
@@ -318,7 +327,8 @@ cudaError_t admit(Request *r) {
     sh.smem = r->generated ? 0 : kTableBytes;
     int per_sm = 0;
     // precision 2 runs the module's current mixed variant (gpu_kin_set_mixed_variant), fixed at admission
-    const uint32_t kp = q.precision == 2 && gpu_kin_get_mixed_variant() == 1 ? 3u : q.precision;
+    const uint32_t mv = gpu_kin_get_mixed_variant();
+    const uint32_t kp = q.precision == 2 && mv == 1 ? 3u : q.precision == 2 && mv == 2 ? 4u : q.precision;
     e = occupancy_chem(r->generated, kp, sh.block, sh.smem, &per_sm);
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;

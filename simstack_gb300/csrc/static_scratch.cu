@@ -51,6 +51,10 @@ cudaError_t launch_air_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_air_p3(uint32_t, uint32_t, uint32_t, int *);
 cudaError_t launch_table_p3(const Shape &, const DevArgs &, cudaStream_t);
 cudaError_t occupancy_table_p3(uint32_t, uint32_t, size_t, int *);
+cudaError_t launch_air_p4(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_air_p4(uint32_t, uint32_t, uint32_t, int *);
+cudaError_t launch_table_p4(const Shape &, const DevArgs &, cudaStream_t);
+cudaError_t occupancy_table_p4(uint32_t, uint32_t, size_t, int *);
 cudaError_t local_air_p0(uint32_t, uint32_t, size_t *);
 cudaError_t local_air_p1(uint32_t, uint32_t, size_t *);
 cudaError_t local_air_p2(uint32_t, uint32_t, size_t *);
@@ -59,6 +63,8 @@ cudaError_t local_table_p0(uint32_t, size_t *);
 cudaError_t local_table_p1(uint32_t, size_t *);
 cudaError_t local_table_p2(uint32_t, size_t *);
 cudaError_t local_table_p3(uint32_t, size_t *);
+cudaError_t local_air_p4(uint32_t, uint32_t, size_t *);
+cudaError_t local_table_p4(uint32_t, size_t *);
 uint64_t air_ops_signature();
 uint32_t module_wait_polls();
 uint32_t module_ir_sweeps();
@@ -160,13 +166,16 @@ SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *me
 
     // the module's default launch shape: CTA-synchronous persistent queue, 128 threads, 255 registers
     const uint32_t kind = 2, variant = 0;
-    // precision 2 runs the module's current mixed variant (gpu_kin_set_mixed_variant)
-    const uint32_t p = L->precision == 2 && gpu_kin_get_mixed_variant() == 1 ? 3u : L->precision;
+    // precision 2 runs the module's current mixed variant (gpu_kin_set_mixed_variant): lane code
+    // 0 FP64, 1 f32 Delta, 2 FP64-state refinement, 3 double-float state, 4 double-float refined
+    const uint32_t mv = gpu_kin_get_mixed_variant();
+    const uint32_t p = L->precision == 2 ? (mv == 0 ? 2u : mv == 1 ? 3u : 4u) : L->precision;
     size_t frame = 0, reserved = 0;
     if (generated) e = p == 0 ? local_air_p0(kind, variant, &frame) : p == 1 ? local_air_p1(kind, variant, &frame)
-                       : p == 2 ? local_air_p2(kind, variant, &frame) : local_air_p3(kind, variant, &frame);
+                       : p == 2 ? local_air_p2(kind, variant, &frame) : p == 3 ? local_air_p3(kind, variant, &frame)
+                       : local_air_p4(kind, variant, &frame);
     else e = p == 0 ? local_table_p0(kind, &frame) : p == 1 ? local_table_p1(kind, &frame)
-             : p == 2 ? local_table_p2(kind, &frame) : local_table_p3(kind, &frame);
+             : p == 2 ? local_table_p2(kind, &frame) : p == 3 ? local_table_p3(kind, &frame) : local_table_p4(kind, &frame);
     if (e == cudaSuccess) e = cudaDeviceGetLimit(&reserved, cudaLimitStackSize);
     if (e != cudaSuccess) return (int32_t)e;
     if (frame > reserved) return (int32_t)cudaErrorLaunchOutOfResources;   // the launch would grow the reservation
@@ -181,15 +190,19 @@ SGB_API int32_t gpu_kin_advance_noalloc(const KinMech *mech, const KinMethod *me
     sh.variant = variant;
     sh.smem = generated ? 0 : kTableBytes;
     if (generated) e = p == 0 ? occupancy_air_p0(kind, variant, sh.block, &per_sm) : p == 1 ? occupancy_air_p1(kind, variant, sh.block, &per_sm)
-                       : p == 2 ? occupancy_air_p2(kind, variant, sh.block, &per_sm) : occupancy_air_p3(kind, variant, sh.block, &per_sm);
+                       : p == 2 ? occupancy_air_p2(kind, variant, sh.block, &per_sm) : p == 3 ? occupancy_air_p3(kind, variant, sh.block, &per_sm)
+                       : occupancy_air_p4(kind, variant, sh.block, &per_sm);
     else e = p == 0 ? occupancy_table_p0(kind, sh.block, sh.smem, &per_sm) : p == 1 ? occupancy_table_p1(kind, sh.block, sh.smem, &per_sm)
-             : p == 2 ? occupancy_table_p2(kind, sh.block, sh.smem, &per_sm) : occupancy_table_p3(kind, sh.block, sh.smem, &per_sm);
+             : p == 2 ? occupancy_table_p2(kind, sh.block, sh.smem, &per_sm) : p == 3 ? occupancy_table_p3(kind, sh.block, sh.smem, &per_sm)
+             : occupancy_table_p4(kind, sh.block, sh.smem, &per_sm);
     if (e != cudaSuccess) return (int32_t)e;
     if (per_sm < 1) per_sm = 1;
     const uint32_t resident = (uint32_t)per_sm * (uint32_t)sms, needed_ctas = (A.lanes + sh.block - 1) / sh.block;
     sh.grid = resident < needed_ctas ? resident : needed_ctas;
-    if (generated) e = p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : p == 2 ? launch_air_p2(sh, A, s) : launch_air_p3(sh, A, s);
-    else e = p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : p == 2 ? launch_table_p2(sh, A, s) : launch_table_p3(sh, A, s);
+    if (generated) e = p == 0 ? launch_air_p0(sh, A, s) : p == 1 ? launch_air_p1(sh, A, s) : p == 2 ? launch_air_p2(sh, A, s)
+                       : p == 3 ? launch_air_p3(sh, A, s) : launch_air_p4(sh, A, s);
+    else e = p == 0 ? launch_table_p0(sh, A, s) : p == 1 ? launch_table_p1(sh, A, s) : p == 2 ? launch_table_p2(sh, A, s)
+             : p == 3 ? launch_table_p3(sh, A, s) : launch_table_p4(sh, A, s);
     if (e != cudaSuccess) return (int32_t)e;
     if (!wait) return 0;
     uint32_t flag = 0;

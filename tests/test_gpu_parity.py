@@ -215,7 +215,8 @@ def mixed_variant(module, request):
     module.set_mixed_variant(before)
 
 
-@pytest.mark.parametrize("mixed_variant", [0, 1], indirect=True, ids=["fp64-refinement", "double-float-state"])
+@pytest.mark.parametrize("mixed_variant", [0, 1, 2], indirect=True,
+                         ids=["fp64-refinement", "double-float-state", "double-float-refined"])
 @pytest.mark.parametrize("method", ["rodas3", "ros3"])
 def test_mixed_matches_model(module, oracle_lib, method, mixed_variant):
     """The GPU mixed kernel (generated code for Rodas3, table walk otherwise)
@@ -232,13 +233,37 @@ def test_mixed_matches_model(module, oracle_lib, method, mixed_variant):
     module.set_tuning()
 
 
+MIXED_BOUND = 1e-5   # max relative error of the mixed path vs the FP64 oracle, every species and cell
+
+
+@pytest.mark.parametrize("duration", [1.0, 10.0], ids=["4096-cells-1s", "4096-cells-10s"])
+def test_mixed_default_within_bound(module, oracle_lib, duration):
+    """The default mixed path (double-float state, FP32 LU preconditioning one
+    double-float refinement sweep per stage) against the FP64 oracle on the first
+    4,096 cells of the seeded humid-air workload: the relative error of EVERY
+    species in every cell, |a - b| / max(|b|, atol) with no species filter, stays
+    <= 1e-5, and every cell takes the FP64 path's steps and rejections. (Its CPU
+    model measures max 2.4e-8 at 1 s and 7.1e-7 at 10 s.)"""
+    module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
+    assert module.mixed_variant() == 2
+    z = sg.air_cells(4096, seed=1)
+    ref = z.copy()
+    module.integrate(z, duration, precision=2)
+    oracle_run(oracle_lib, ref, duration)
+    sig, floored = mixed_errors(z, ref)
+    assert np.isfinite(floored).all() and z["failed"].max() == 0.0
+    assert floored.max() <= MIXED_BOUND, floored.max()
+    assert np.array_equal(z["steps"], ref["steps"]) and np.array_equal(z["rejects"], ref["rejects"])
+
+
 @pytest.mark.parametrize("mixed_variant", [0, 1], indirect=True, ids=["fp64-refinement", "double-float-state"])
 def test_mixed_precision_accuracy(module, oracle_lib, mixed_variant):
-    """Mixed path vs the FP64 oracle on 4,096 seeded humid-air cells (1 s, rtol 1e-4). Bounds
-    (measured on the CPU models of the mixed paths: max 7.3e-5 both, p99 3.9e-7
-    (variant 0) and 8.7e-7 (variant 1), floored max 3.1e-4 and 1.3e-3):
-    species >= 1e-6 ppm: max rel err < 1e-4, p99 < 1e-6; every entry with the
-    error floored at atol: max < 2e-3; no failed cells."""
+    """The two earlier, faster-per-step mixed variants (kept as options, not the
+    default: neither meets the 1e-5 bound) vs the FP64 oracle on 4,096 seeded
+    humid-air cells (1 s, rtol 1e-4). Bounds (measured on their CPU models: max
+    7.3e-5 both, p99 3.9e-7 (variant 0) and 8.7e-7 (variant 1), floored max 3.1e-4
+    and 1.3e-3): species >= 1e-6 ppm: max rel err < 1e-4, p99 < 1e-6; every entry
+    with the error floored at atol: max < 2e-3; no failed cells."""
     module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
     z = sg.air_cells(4096, seed=1)
     ref = z.copy()
@@ -306,7 +331,7 @@ def test_table_path_near_capacity(module, oracle_lib):
 def test_full_size_sampled_cells(module, oracle_lib):
     """The full 1,048,576-cell x 10 s workload on the GPU; 256 cells sampled across
     the batch checked against the oracle (cells are independent): FP64 bit for bit,
-    mixed within its bounds."""
+    the default mixed path within 1e-5 on every species."""
     module.reset_arena()
     module.set_mech(sg.Model.air().kinmech(), sg.method("rodas3"), sg.control())
     cells = 1 << 20
@@ -328,5 +353,5 @@ def test_full_size_sampled_cells(module, oracle_lib):
     got = sg.ZoneBlock(17, 44, 256)
     got["y"][...] = out[2]["y"][:, pick]
     sig, floored = mixed_errors(got, ref)
-    assert np.quantile(sig, 0.99) < 1e-6 and out[2]["failed"].max() == 0.0
+    assert floored.max() <= MIXED_BOUND and out[2]["failed"].max() == 0.0, floored.max()
     module.reset_arena()

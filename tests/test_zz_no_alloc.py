@@ -46,10 +46,15 @@ def _advance_twice_queue(z, base, precision, duration):
         assert rc == 0, L.gpu_error_string(rc).decode()
 
 
+TABLE_FRAME_BYTES = 10752   # the table-driven kernels' largest per-thread frame (the generated ones fit gpu_init's 3,840)
+
+
 def _setup(method):
     mod = sg.Module(0, 256 << 20)
     km, meth, ctl = sg.Model.air().kinmech(), sg.method(method), sg.control()
     mod.set_mech(km, meth, ctl)
+    if method != "rodas3":   # set-up for the table-driven kernels: a stack reservation that covers their frame
+        assert sg.lib().gpu_stack_limit(TABLE_FRAME_BYTES, None) == 0
     return mod, km, meth, ctl
 
 
