@@ -69,8 +69,8 @@ def parse():
     ap.add_argument("--requests", type=int, default=48, help="serve-poisson200: requests in the served sample")
     ap.add_argument("--tuning", default=None,
                     help="--profile-case: launch shape block,variant,ctas_per_sm of the CTA-synchronous queue kernel")
-    ap.add_argument("--mixed-variant", type=int, choices=[0, 1], default=None,
-                    help="--profile-case mixed: 0 = FP64 state with refinement, 1 = double-float state (default)")
+    ap.add_argument("--mixed-variant", type=int, choices=[0, 1, 2], default=None,
+                    help="--profile-case mixed: 0 = FP64 state with refinement, 1 = double-float state, 2 = double-float state with refined stages (default)")
     ap.add_argument("--fp64-cells", type=int, default=1216,
                     help="mech200-65536x10s: cells of the FP64 comparison sample (the first cells of the workload)")
     ap.add_argument("--profile-case", choices=["f64", "mixed", "f32", "coop-f64", "coop-mixed"], default=None,
@@ -197,7 +197,13 @@ def flops_per_step(model) -> dict:
     combo = 2 * 13 * n                                           # Rodas3 nonzero a, c, m, e: 3 + 6 + 3 + 1 FMAs per species
     control = 8 * n                                              # scale fma, divide, square fma, max/abs, clamp
     total = 4 * fun + jac + lu + 4 * solve + combo + control
-    return {"fun": fun, "neg_jac": jac, "factor": lu, "solve": solve, "total": total}
+    # the FP64 path executes one RHS evaluation fewer than the count above: Rodas3's second
+    # stage point is y itself, so f(y) is reused (bit for bit)
+    return {"fun": fun, "neg_jac": jac, "factor": lu, "solve": solve, "total": total, "executed_f64": total - fun}
+
+
+FP64_FMA_PER_CLK_SM = 2      # GB300: FP64 FMAs per clock per SM
+FP32_LANES_SM = 128          # FP32 lanes per SM
 
 
 # DRAM bytes (read + write) per attempted cell-step of the queue kernels, from one ncu capture each
@@ -208,6 +214,16 @@ def flops_per_step(model) -> dict:
 # the bench scales it to its own launch.
 DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 2045.3}
 PIPELINE_CHUNKS = (2, 4)   # lane-chunk counts tried for the pipelined end-to-end call (8 and 16 measured slower)
+
+
+def mixed_errors(a: np.ndarray, b: np.ndarray, atol: float = 6.02214076e8) -> dict:
+    """Max and p99 of |a - b| / max(|b|, atol) over every entry (species x cells), no filter;
+    and the same over species at or above 1e-3 ppm of their cell's total density (the
+    threshold of the reference's own f32-vs-f64 product check, test_kinetics.cpp:316)."""
+    rel = np.abs(a - b) / np.maximum(np.abs(b), atol)
+    big = b >= 1e-9 * b.sum(axis=0)
+    return {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
+            "max_species_above_1e-3_ppm": float(rel[big].max()) if big.any() else 0.0}
 
 
 def hbm_bytes_per_cell(n: int, R: int) -> int:
@@ -280,7 +296,7 @@ def cpu_baseline(cells_total: int, duration: float, seed: int, target_s: float, 
     out = {"value": cells / wall, "unit": "cell-integrations/s", "cores": threads, "kind": kind,
            "sample": f"first {cells} cells of the workload (same seeded inputs), {duration:g} s each, {threads} host "
                      f"threads, {wall:.1f} s wall; {CPU_PATHS[kind]}; rate constants from the {rates}",
-           "wall_s": wall, "cells": cells}
+           "wall_s": wall, "cells": cells, "y": block["y"][:, :cells].copy()}
     if with_port and kind == "reference":   # the restatement on the same sample, for comparison
         block, P, _ = O.air_block(cells, seed=seed)
         wall_p = _cpu_advance("port", block, P, duration, threads)
@@ -464,34 +480,36 @@ def run_ours(args):
     L.gpu_host_unregister(zz.data.ctypes.data)
     L.gpu_host_unregister(z.data.ctypes.data)
 
-    # the mixed path's other variant (FP64 state + FP64-residual refinement), for comparison
+    # the mixed path's faster, less accurate variant (double-float state, FP32 stage solves without
+    # refinement), for comparison
     tuned_mx = mod.tuning(2)
     variant_default = mod.mixed_variant()
-    mod.set_mixed_variant(0)
+    mod.set_mixed_variant(1)
     restore()
     launch.precision = 2
-    t_v0 = mod.autotune(launch, kind=2)
-    wall_v0, kern_v0, _ = timed_pass(2, args.steps, 1)
-    zv0 = z.copy()
-    mod.download(zv0, work)
+    t_v1 = mod.autotune(launch, kind=2)
+    wall_v1, kern_v1, _ = timed_pass(2, args.steps, 1)
+    zv1 = z.copy()
+    mod.download(zv1, work)
     mod.set_mixed_variant(variant_default)
     mod.set_tuning(kind=tuned_mx.kind, block=tuned_mx.block, variant=tuned_mx.variant, ctas_per_sm=tuned_mx.chunk)
 
-    # accuracy of the mixed result on this batch vs the FP64 result (bit-identical to the oracle)
-    atol = sg.ATOL_1E12_MOLAR
-    ya, yb = zm["y"][:, :cells], zc["y"][:, :cells]
-    rel = np.abs(ya - yb) / np.maximum(np.abs(yb), atol)
-    sig_mask = yb >= 1e-12 * yb.sum(axis=0)
-    with np.errstate(all="ignore"):
-        rel_sig = (np.abs(ya - yb) / np.abs(yb))[sig_mask]
-    flips = float(np.mean((zm["steps"][:cells] != zc["steps"][:cells]) | (zm["rejects"][:cells] != zc["rejects"][:cells])))
-    with np.errstate(all="ignore"):
-        rel_sig_v0 = (np.abs(zv0["y"][:, :cells] - yb) / np.abs(yb))[sig_mask]
+    # accuracy of the mixed result on this batch vs the FP64 result (bit-identical to the oracle):
+    # every species of every cell, relative to max(|FP64|, atol), no filter
+    yb = zc["y"][:, :cells]
+    err_all = mixed_errors(zm["y"][:, :cells], yb)
+    err_v1 = mixed_errors(zv1["y"][:, :cells], yb)
+    flips = int(np.sum((zm["steps"][:cells] != zc["steps"][:cells]) | (zm["rejects"][:cells] != zc["rejects"][:cells])))
 
-    # roofline peaks measured live on this device
+    # roofline denominators: per-SM issue rates x SMs x the median SM clock sampled under load
+    # (FP64: 2 FMA per clock per SM; FP32: 128 lanes), the live FMA probes recorded beside
     dfma = mod.probe(0)
     ffma = mod.probe(1)
     hbm_peak, hbm_src = measured_hbm_peak()
+    sms = int(mod.info.multiprocessors)
+    clk_hz = (clk.get("sm_mhz") or 2070.0) * 1e6
+    fp64_peak = sms * FP64_FMA_PER_CLK_SM * 2 * clk_hz / 1e12
+    fp32_peak = sms * FP32_LANES_SM * 2 * clk_hz / 1e12
 
     ms64 = float(np.mean(kern64))
     msmx = float(np.mean(kernmx))
@@ -503,22 +521,52 @@ def run_ours(args):
     total_cells = cells * world
     v64 = total_cells / (ms_step64 * 1e-3)
     vmx = total_cells / (ms_stepmx * 1e-3)
-    alg_flops = steps_total * flops["total"]
-    ach64 = alg_flops / (ms64 * 1e-3) / 1e12
-    achmx = alg_flops / (msmx * 1e-3) / 1e12
-    fp64_peak = 2.0 * dfma / 1e12
-    fp32_peak = 2.0 * ffma / 1e12
+    alg64 = steps_total * flops["total"] / (ms64 * 1e-3) / 1e12
+    exe64 = steps_total * flops["executed_f64"] / (ms64 * 1e-3) / 1e12
+    fp32_ops = MIXED_FP32_FLOPS_PER_CELL_STEP * steps_total / (msmx * 1e-3) / 1e12
     alg_bytes = cells * hbm_bytes_per_cell(n, R)
     head = "mixed" if args.precision == "mixed" else "f64"
     ms_head = msmx if head == "mixed" else ms64
-    cpu = None
+    cpu, subset = None, None
     if rank == 0 and not args.no_cpu:
         cpu = cpu_baseline(cells, args.duration, args.seed, args.cpu_seconds)
+        m = cpu.pop("cells")
         cpu.pop("wall_s")
-        cpu.pop("cells")
+        ref_y = cpu.pop("y")
+        subset = {"cells": m,
+                  "fp64_bit_identical": bool(np.array_equal(zc["y"][:, :m], ref_y)),
+                  "mixed_rel_err": mixed_errors(zm["y"][:, :m], ref_y),
+                  "against": "the CPU baseline's own run of the first cells (" + cpu["kind"] + " solver)"}
     if rank != 0:
         grp.close()
         return
+    if head == "mixed":
+        roof = {"bound": "fp32", "achieved": fp32_ops, "peak": fp32_peak, "unit": "TFLOP/s", "frac": fp32_ops / fp32_peak,
+                "of": "measured SM clock x 152 SMs x 128 FP32 lanes x 2 (FMA)",
+                "work": "FP32 flops executed per cell-step (ncu instruction counts of the kernel: FADD + FMUL + 2 FFMA, "
+                        f"{MIXED_FP32_FLOPS_PER_CELL_STEP:.0f}) x attempted cell-steps"}
+    else:
+        roof = {"bound": "fp64", "achieved": exe64, "peak": fp64_peak, "unit": "TFLOP/s", "frac": exe64 / fp64_peak,
+                "of": "measured SM clock x 152 SMs x 2 FP64 FMA per clock x 2",
+                "work": f"FP64 flops executed per step ({flops['executed_f64']}) x attempted cell-steps"}
+    roof.update({
+        "traffic": DRAM_BYTES_PER_CELL_STEP[head] * steps_total,
+        "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per launch: the per-cell-step figure of one "
+                        "ncu capture (262,144 cells x 0.5 s) x this launch's attempted cell-steps; local-memory "
+                        "traffic, not algorithmic bytes",
+        "sm_count": sms, "sm_mhz": clk.get("sm_mhz"),
+        "probes": {"fp64_fma_tflops": 2 * dfma / 1e12, "fp32_fma_tflops": 2 * ffma / 1e12,
+                   "note": "gpu_probe_throughput, FMA chains on every SM, in this run"},
+        "fp64_path": {"algorithmic": alg64, "executed": exe64, "peak": fp64_peak, "frac_algorithmic": alg64 / fp64_peak,
+                      "frac_executed": exe64 / fp64_peak, "algorithmic_flops_per_step": flops["total"],
+                      "executed_flops_per_step": flops["executed_f64"],
+                      "note": "algorithmic: 4 RHS per Rodas3 step; executed: 3 (stage 2 reuses f(y))"},
+        "mixed_path": {"fp32_achieved": fp32_ops, "fp32_peak": fp32_peak, "frac_of_fp32_peak": fp32_ops / fp32_peak,
+                       "fp64_equivalent_achieved": steps_total * flops["total"] / (msmx * 1e-3) / 1e12,
+                       "fp64_equivalent_frac": steps_total * flops["total"] / (msmx * 1e-3) / 1e12 / fp64_peak},
+        "hbm": {"achieved": alg_bytes / (ms_head * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
+                "frac": alg_bytes / (ms_head * 1e-3) / 1e9 / hbm_peak, "peak_source": hbm_src,
+                "algorithmic_bytes_per_cell": hbm_bytes_per_cell(n, R)}})
     line = {
         "metric": "cell-integrations/s",
         "value": vmx if head == "mixed" else v64,
@@ -537,47 +585,22 @@ def run_ours(args):
         "fp64": {"value": v64, "ms_per_step": ms_step64, "kernel_ms": ms64,
                  "parity": "bit-identical to the reference CPU solver (tests/test_gpu_parity.py)"},
         "mixed": {"value": vmx, "ms_per_step": ms_stepmx, "kernel_ms": msmx, "speedup_vs_fp64": v64 and vmx / v64,
-                  "rel_err_vs_fp64": {"max": float(rel_sig.max()), "p99": float(np.quantile(rel_sig, 0.99)),
-                                      "definition": "|a-b|/|b| over species >= 1e-6 ppm of the cell total, all cells"},
-                  "rel_err_vs_fp64_atol_floored": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
-                                                   "definition": "|a-b|/max(|b|, atol) over every species and cell"},
+                  "rel_err_vs_fp64": dict(err_all, definition="|a-b| / max(|b|, atol) over every species of every cell, "
+                                                             "no filter; b = the FP64 path (the reference's bits)"),
+                  "rel_err_vs_reference_cpu_subset": subset,
                   "cells_with_different_step_counts": flips,
-                  "reference_for_errors": "the FP64 path on the same batch, bit-identical to the reference CPU solver",
-                  "variant": "double-float state (hi+lo FP32 pairs), FP32 Jacobian / LU / stage vectors / solves, "
-                             "double-float stage right-hand sides; FP64 only in the scalar step controller"
-                             if variant_default == 1 else "FP64 state, FP32 LU, one FP64-residual refinement sweep",
-                  "other_variant": {"variant": "FP64 state, FP32 Jacobian / LU / solves, one FP64-residual refinement "
-                                               "sweep per stage, double-float f(y)" if variant_default == 1 else
-                                               "double-float state",
-                                    "kernel_ms": float(np.mean(kern_v0)),
-                                    "value": total_cells / (grp.max(wall_v0 / args.steps * 1e3) * 1e-3),
-                                    "speedup_vs_fp64": ms64 / float(np.mean(kern_v0)),
-                                    "rel_err_vs_fp64": {"max": float(rel_sig_v0.max()),
-                                                        "p99": float(np.quantile(rel_sig_v0, 0.99))},
-                                    "tuning": {"block": t_v0.block, "variant": t_v0.variant, "ctas_per_sm": t_v0.chunk}}},
+                  "variant": "double-float state (hi+lo FP32 pairs); FP32 Jacobian and LU of W precondition one "
+                             "double-float refinement sweep per stage (residual b - W x with J x formed reaction by "
+                             "reaction); stage points, right-hand sides, stage vectors, y_new and the error norm in "
+                             "double-float; FP64 only in the scalar step controller",
+                  "other_variant": {"variant": "double-float state, FP32 stage solves without refinement",
+                                    "kernel_ms": float(np.mean(kern_v1)),
+                                    "value": total_cells / (grp.max(wall_v1 / args.steps * 1e3) * 1e-3),
+                                    "speedup_vs_fp64": ms64 / float(np.mean(kern_v1)),
+                                    "rel_err_vs_fp64": err_v1,
+                                    "tuning": {"block": t_v1.block, "variant": t_v1.variant, "ctas_per_sm": t_v1.chunk}}},
         "steps_per_cell": {"mean": steps_total / cells, "failed_cells": failed},
-        "roofline": {"bound": "fp64" if head == "f64" else "fp32",
-                     "achieved": ach64 if head == "f64" else achmx,
-                     "peak": fp64_peak if head == "f64" else fp32_peak,
-                     "unit": "TFLOP/s",
-                     "frac": ach64 / fp64_peak if head == "f64" else achmx / fp32_peak,
-                     "traffic": DRAM_BYTES_PER_CELL_STEP[head] * steps_total,
-                     "traffic_note": "dram__bytes_read.sum + dram__bytes_write.sum per launch: the per-cell-step "
-                                     "figure of one ncu capture (262,144 cells x 0.5 s) x this launch's attempted "
-                                     "cell-steps (FP64-path counts); local-memory spills, not algorithmic bytes",
-                     "peak_source": "FMA throughput measured in this run (gpu_probe_throughput kind 0 FP64, "
-                                    "kind 1 FP32), x2 flops",
-                     "algorithmic_flops_per_step": flops["total"],
-                     "note": "algorithmic flops = FP64 path step count (= the oracle's) x flops per Rodas3 step; "
-                             "the mixed path does them on the FP32 pipe, in double-float where precision needs it "
-                             "(several FP32 instructions per algorithmic flop), so its fraction of the FP32 peak "
-                             "understates the pipe's use; mixed_path.frac_of_fp64_peak is the FP64-equivalent rate",
-                     "fp64_path": {"achieved": ach64, "frac": ach64 / fp64_peak},
-                     "mixed_path": {"achieved": achmx, "frac_of_fp64_peak": achmx / fp64_peak,
-                                    "frac_of_fp32_peak": achmx / fp32_peak, "fp32_peak": fp32_peak},
-                     "hbm": {"achieved": alg_bytes / (ms_head * 1e-3) / 1e9, "peak": hbm_peak, "unit": "GB/s",
-                             "frac": alg_bytes / (ms_head * 1e-3) / 1e9 / hbm_peak, "peak_source": hbm_src,
-                             "algorithmic_bytes_per_cell": hbm_bytes_per_cell(n, R)}},
+        "roofline": roof,
         "cpu_baseline": cpu,
         "e2e": {"value": total_cells / (e2e_ms * 1e-3), "unit": "cell-integrations/s",
                 "h2d_bytes_per_step": block_bytes, "d2h_bytes_per_step": z.mutable_rows * z.padded * 8,

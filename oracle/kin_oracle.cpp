@@ -1274,30 +1274,83 @@ static inline Df2 df_times_coef(Df2 a, double c) {   // method coefficients a_ij
     return df_mul(a, df_from(c));
 }
 
-// v = J(y) x, reaction by reaction: d rate_r = sum_p k_r (prod_{q != p} y[q]) x[q_p], each
-// term multiplied out from k_r (which keeps products of large number densities in FP32
-// range), then v[s] += net_{r,s} d rate_r in reaction order (the order of eval_fun_df).
-static void eval_jvp_df(const Mechanism &m, const Df2 *k, const Df2 *y, const float *x, Df2 *v) {
-    for (u32 s = 0; s < m.n(); ++s) v[s] = Df2{0.0f, 0.0f};
+// Lazily normalised double-float arithmetic for the refined variant's sums: df_acc adds a
+// pair to an accumulator whose hi holds the rounded running sum and whose lo collects the
+// low parts and every two-sum rounding error (8 operations instead of df_add's 11); the
+// products skip their final renormalisation (|lo| stays within a few ulp of hi); a sum is
+// normalised once, with a two-sum, when it is complete.
+static inline Df2 df_acc(Df2 a, Df2 t) {
+    float s = a.hi + t.hi;
+    float bb = s - a.hi;
+    float e = (a.hi - (s - bb)) + (t.hi - bb);
+    return Df2{s, a.lo + (t.lo + e)};
+}
+static inline Df2 df_mul_u(Df2 a, Df2 b) {
+    float p = a.hi * b.hi;
+    float e = std::fma(a.hi, b.hi, -p);
+    e = std::fma(a.hi, b.lo, e);
+    e = std::fma(a.lo, b.hi, e);
+    return Df2{p, e};
+}
+static inline Df2 df_mul_fu(Df2 a, float b) {
+    float p = a.hi * b;
+    float e = std::fma(a.hi, b, -p);
+    e = std::fma(a.lo, b, e);
+    return Df2{p, e};
+}
+static inline Df2 df_norm(Df2 a) { return df_two_sum(a.hi, a.lo); }
+static inline Df2 df_times_coef_u(Df2 a, double c) {   // method coefficients, lazily normalised product
+    if (c == 1.0) return a;
+    if (c == -1.0 || c == 2.0 || c == -2.0 || c == 4.0 || c == -4.0 || c == 0.5 || c == -0.5) return df_scale(a, (float)c);
+    return df_mul_u(a, df_from(c));
+}
+static inline Df2 df_times_int_u(Df2 a, int c) {
+    if (c == 1) return a;
+    if (c == -1 || c == 2 || c == -2 || c == 4 || c == -4) return df_scale(a, (float)c);
+    return df_mul_u(a, Df2{(float)c, 0.0f});
+}
+
+// f(y) in lazily normalised double-float: the terms of eval_fun_df in the same order.
+static void eval_fun_dfl(const Mechanism &m, const Df2 *k, const Df2 *src, const Df2 *y, Df2 *f) {
+    for (u32 s = 0; s < m.n(); ++s) f[s] = src[s];
+    for (u32 r = 0; r < m.R(); ++r) {
+        const Reaction &rx = m.reactions[r];
+        Df2 rate = k[r];
+        for (u32 p = 0; p < rx.reactant_count; ++p) rate = df_mul_u(rate, y[rx.reactant[p]]);
+        for (u32 e = 0; e < rx.net_count; ++e) f[rx.net_species[e]] = df_acc(f[rx.net_species[e]], df_times_int_u(rate, rx.net_coef[e]));
+    }
+    for (u32 s = 0; s < m.n(); ++s) f[s] = df_norm(f[s]);
+}
+
+// The refinement residual, whole: r = b - ghinv x + J(y) x, accumulated per species from
+// b - ghinv x through the terms of J(y) x in reaction order: d rate_r = sum_p k_r (prod_{q != p}
+// y[q]) x[q_p], each term multiplied out from k_r (which keeps products of large number
+// densities in FP32 range), then r_s += net_{r,s} d rate_r (no intermediate J x vector);
+// returns the FP32 rounding of each r_s as the right-hand side of the correction solve.
+static void eval_residual_df(const Mechanism &m, const Df2 *k, const Df2 *y, const float *x, const Df2 *b, Df2 gd, float *x2) {
+    const u32 n = m.n();
+    std::vector<Df2> acc(n);
+    for (u32 s = 0; s < n; ++s) acc[s] = df_acc(b[s], df_neg(df_mul_fu(gd, x[s])));
     for (u32 r = 0; r < m.R(); ++r) {
         const Reaction &rx = m.reactions[r];
         Df2 drate{0.0f, 0.0f};
         for (u32 p = 0; p < rx.reactant_count; ++p) {
             Df2 t = k[r];
             for (u32 q = 0; q < rx.reactant_count; ++q)
-                if (q != p) t = df_mul(t, y[rx.reactant[q]]);
-            t = df_mul_f(t, x[rx.reactant[p]]);
-            drate = p == 0 ? t : df_add(drate, t);
+                if (q != p) t = df_mul_u(t, y[rx.reactant[q]]);
+            t = df_mul_fu(t, x[rx.reactant[p]]);
+            drate = p == 0 ? t : df_acc(drate, t);
         }
-        for (u32 e = 0; e < rx.net_count; ++e) v[rx.net_species[e]] = df_add(v[rx.net_species[e]], df_times_int(drate, rx.net_coef[e]));
+        for (u32 e = 0; e < rx.net_count; ++e) acc[rx.net_species[e]] = df_acc(acc[rx.net_species[e]], df_times_int_u(drate, rx.net_coef[e]));
     }
+    for (u32 s = 0; s < n; ++s) x2[s] = acc[s].hi + acc[s].lo;
 }
 
 static void integrate_mixed_ir(const Mechanism &m, const Method &me, const Control &ctl, Df2 *y, double &t, double t_end,
                                double &h, Stats<double> &st, MixedWork &w) {
     const u32 n = m.n();
     std::vector<float> yhi(n), x(n), x2(n);
-    std::vector<Df2> Y(n), fy(n), b(n), jv(n), kd((size_t)4 * n), ynew(n);
+    std::vector<Df2> Y(n), fy(n), b(n), kd((size_t)4 * n), ynew(n);
     Df2 *K[4] = {kd.data(), kd.data() + n, kd.data() + 2 * n, kd.data() + 3 * n};
     float *a = w.a.data();
     const Df2 rtol = df_from(ctl.rtol), atol = df_from(ctl.atol);
@@ -1317,7 +1370,7 @@ static void integrate_mixed_ir(const Mechanism &m, const Method &me, const Contr
         const double ghinv = 1.0 / (hs * me.gamma0), hinv = 1.0 / hs;
         const Df2 gd = df_from(ghinv);
 
-        eval_fun_df(m, w.kd.data(), w.sd.data(), y, fy.data());
+        eval_fun_dfl(m, w.kd.data(), w.sd.data(), y, fy.data());
         for (u32 s = 0; s < n; ++s) yhi[s] = y[s].hi;
         eval_neg_jac(m, w.k32.data(), yhi.data(), a);
         factor(m, (float)ghinv, a);
@@ -1331,23 +1384,27 @@ static void integrate_mixed_ir(const Mechanism &m, const Method &me, const Contr
                     double av = me.a[packed + j];
                     if (av == 0.0) continue;
                     moved = true;
-                    for (u32 s = 0; s < n; ++s) Y[s] = df_add(Y[s], df_times_coef(K[j][s], av));
+                    for (u32 s = 0; s < n; ++s) Y[s] = df_acc(Y[s], df_times_coef_u(K[j][s], av));
                 }
-                if (moved) eval_fun_df(m, w.kd.data(), w.sd.data(), Y.data(), fy.data());
-                else eval_fun_df(m, w.kd.data(), w.sd.data(), y, fy.data());
+                if (moved) {
+                    for (u32 s = 0; s < n; ++s) Y[s] = df_norm(Y[s]);
+                    eval_fun_dfl(m, w.kd.data(), w.sd.data(), Y.data(), fy.data());
+                } else {
+                    eval_fun_dfl(m, w.kd.data(), w.sd.data(), y, fy.data());
+                }
             }
             for (u32 s = 0; s < n; ++s) b[s] = fy[s];
             for (u32 j = 0; j < stg; ++j) {
                 double c = me.c[packed + j];
                 if (c == 0.0) continue;
                 const Df2 ch = df_from(c * hinv);
-                for (u32 s = 0; s < n; ++s) b[s] = df_add(b[s], df_mul(ch, K[j][s]));
+                for (u32 s = 0; s < n; ++s) b[s] = df_acc(b[s], df_mul_u(ch, K[j][s]));
             }
+            for (u32 s = 0; s < n; ++s) b[s] = df_norm(b[s]);
             for (u32 s = 0; s < n; ++s) x[s] = b[s].hi;
             solve(m, a, x.data());
             // one refinement sweep: r = b - ghinv x + J x in double-float, x += W32^-1 r
-            eval_jvp_df(m, w.kd.data(), y, x.data(), jv.data());
-            for (u32 s = 0; s < n; ++s) x2[s] = df_add(df_add(b[s], df_neg(df_mul_f(gd, x[s]))), jv[s]).hi;
+            eval_residual_df(m, w.kd.data(), y, x.data(), b.data(), gd, x2.data());
             solve(m, a, x2.data());
             for (u32 s = 0; s < n; ++s) K[stg][s] = df_two_sum(x[s], x2[s]);
         }
@@ -1357,12 +1414,14 @@ static void integrate_mixed_ir(const Mechanism &m, const Method &me, const Contr
             Df2 yn = y[s], ye{0.0f, 0.0f};
             bool first_e = true;
             for (u32 stg = 0; stg < me.stages; ++stg) {
-                if (me.m[stg] != 0.0) yn = df_add(yn, df_times_coef(K[stg][s], me.m[stg]));
+                if (me.m[stg] != 0.0) yn = df_acc(yn, df_times_coef_u(K[stg][s], me.m[stg]));
                 if (me.e[stg] != 0.0) {
-                    ye = first_e ? df_times_coef(K[stg][s], me.e[stg]) : df_add(ye, df_times_coef(K[stg][s], me.e[stg]));
+                    ye = first_e ? df_times_coef_u(K[stg][s], me.e[stg]) : df_acc(ye, df_times_coef_u(K[stg][s], me.e[stg]));
                     first_e = false;
                 }
             }
+            yn = df_norm(yn);
+            ye = df_norm(ye);
             Df2 ay = df_abs(y[s]), an = df_abs(yn);
             const Df2 scale = df_add(df_mul(rtol, df_less(ay, an) ? an : ay), atol);
             const float inv = 1.0f / scale.hi;

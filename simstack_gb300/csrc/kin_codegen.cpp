@@ -25,6 +25,13 @@
 
 using namespace sgb;
 
+// acc[s] += c * v with the lazily normalised accumulation (exact scaling for +-1, +-2, +-4).
+static void emit_lazy_term(FILE *f, uint32_t s, int c, const char *v) {
+    if (c == 1) fprintf(f, "          acc[%u] = df_acc(acc[%u], %s);\n", s, s, v);
+    else if (c == -1 || c == 2 || c == -2 || c == 4 || c == -4) fprintf(f, "          acc[%u] = df_acc(acc[%u], df_scale(%s, %d.0f));\n", s, s, v, c);
+    else fprintf(f, "          acc[%u] = df_acc(acc[%u], df_mul_u(%s, Df{%d.0f, 0.0f}));\n", s, s, v, c);
+}
+
 static void emit_ops(FILE *f, Model &m, const char *name) {
     const Symbolic &S = m.sym;
     const uint32_t n = m.n(), R = m.R();
@@ -82,12 +89,14 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
     for (uint32_t s = 0; s < n; ++s) fprintf(f, "        fhi[%u] = acc[%u].hi; flo[%u] = acc[%u].lo;\n", s, s, s, s);
     fprintf(f, "    }\n\n");
 
-    // mixed variant 2: v = J(y) x in double-float, reaction by reaction: d rate_r = sum_p
-    // k_r (prod_{q != p} y_q) x_p with every term multiplied out from k_r (keeps products of
-    // large number densities in FP32 range), then v_s += net_{r,s} d rate_r in reaction order
-    fprintf(f, "    static __device__ __forceinline__ void jvp_df(const float *__restrict__ khi, const float *__restrict__ klo, const float *__restrict__ yhi, const float *__restrict__ ylo, const float *__restrict__ x, float *__restrict__ vhi, float *__restrict__ vlo) {\n");
+    // mixed variant 2: the refinement residual r = b - ghinv x + J(y) x in lazily normalised
+    // double-float, accumulated per species from b - ghinv x through J x's terms reaction by
+    // reaction: d rate_r = sum_p k_r (prod_{q != p} y_q) x_p, each term multiplied out from k_r
+    // (keeps products of large number densities in FP32 range), then r_s += net_{r,s} d rate_r;
+    // out: the FP32 rounding of r, the right-hand side of the correction solve
+    fprintf(f, "    static __device__ __forceinline__ void residual_df(const float *__restrict__ khi, const float *__restrict__ klo, const float *__restrict__ yhi, const float *__restrict__ ylo, const float *__restrict__ x, const float *__restrict__ bhi, const float *__restrict__ blo, Df g, float *__restrict__ r) {\n");
     fprintf(f, "        Df acc[%u];\n", n);
-    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        acc[%u] = Df{0.0f, 0.0f};\n", s);
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        acc[%u] = df_acc(Df{bhi[%u], blo[%u]}, df_neg(df_mul_fu(g, x[%u])));\n", s, s, s, s);
     for (uint32_t r = 0; r < R; ++r) {
         const Reaction &rx = m.reactions[r];
         if (rx.reactants.empty()) continue;
@@ -95,20 +104,28 @@ static void emit_ops(FILE *f, Model &m, const char *name) {
         for (size_t p = 0; p < rx.reactants.size(); ++p) {
             fprintf(f, "          { Df t = Df{khi[%u], klo[%u]};", r, r);
             for (size_t q = 0; q < rx.reactants.size(); ++q)
-                if (q != p) fprintf(f, " t = df_mul(t, Df{yhi[%u], ylo[%u]});", rx.reactants[q], rx.reactants[q]);
-            fprintf(f, " t = df_mul_f(t, x[%u]);", rx.reactants[p]);
-            fprintf(f, p == 0 ? " drate = t; }\n" : " drate = df_add(drate, t); }\n");
+                if (q != p) fprintf(f, " t = df_mul_u(t, Df{yhi[%u], ylo[%u]});", rx.reactants[q], rx.reactants[q]);
+            fprintf(f, " t = df_mul_fu(t, x[%u]);", rx.reactants[p]);
+            fprintf(f, p == 0 ? " drate = t; }\n" : " drate = df_acc(drate, t); }\n");
         }
-        for (auto &e : rx.net) {
-            int c = e.second;
-            if (c == 1) fprintf(f, "          acc[%u] = df_add(acc[%u], drate);\n", e.first, e.first);
-            else if (c == -1 || c == 2 || c == -2 || c == 4 || c == -4)
-                fprintf(f, "          acc[%u] = df_add(acc[%u], df_scale(drate, %d.0f));\n", e.first, e.first, c);
-            else fprintf(f, "          acc[%u] = df_add(acc[%u], df_mul(drate, Df{%d.0f, 0.0f}));\n", e.first, e.first, c);
-        }
+        for (auto &e : rx.net) emit_lazy_term(f, e.first, e.second, "drate");
         fprintf(f, "        }\n");
     }
-    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        vhi[%u] = acc[%u].hi; vlo[%u] = acc[%u].lo;\n", s, s, s, s);
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        r[%u] = acc[%u].hi + acc[%u].lo;\n", s, s, s);
+    fprintf(f, "    }\n\n");
+
+    // fun in lazily normalised double-float (mixed variant 2): fun_df's terms in fun_df's order
+    fprintf(f, "    static __device__ __forceinline__ void fun_dfl(const float *__restrict__ khi, const float *__restrict__ klo, const float *__restrict__ shi, const float *__restrict__ slo, const float *__restrict__ yhi, const float *__restrict__ ylo, float *__restrict__ fhi, float *__restrict__ flo) {\n");
+    fprintf(f, "        Df acc[%u];\n", n);
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        acc[%u] = Df{shi[%u], slo[%u]};\n", s, s, s);
+    for (uint32_t r = 0; r < R; ++r) {
+        const Reaction &rx = m.reactions[r];
+        fprintf(f, "        { Df rate = Df{khi[%u], klo[%u]};\n", r, r);
+        for (uint32_t q : rx.reactants) fprintf(f, "          rate = df_mul_u(rate, Df{yhi[%u], ylo[%u]});\n", q, q);
+        for (auto &e : rx.net) emit_lazy_term(f, e.first, e.second, "rate");
+        fprintf(f, "        }\n");
+    }
+    for (uint32_t s = 0; s < n; ++s) fprintf(f, "        { const Df v = df_norm(acc[%u]); fhi[%u] = v.hi; flo[%u] = v.lo; }\n", s, s, s);
     fprintf(f, "    }\n\n");
 
     // mixed path: FP32 RHS increment f(y + d) - f(y) from the exact expansion

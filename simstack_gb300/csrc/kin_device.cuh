@@ -923,17 +923,50 @@ __device__ __forceinline__ Df df_two_sum(float a, float b) {   // exact a + b, n
     const float e = (a - (s - bb)) + (b - bb);
     return Df{s, e};
 }
+// Lazily normalised double-float arithmetic for the long sums: df_acc adds a pair to an
+// accumulator whose hi holds the rounded running sum and whose lo collects the low parts and
+// every two-sum rounding error (8 FP32 operations instead of df_add's 11); the products skip
+// their final renormalisation (|lo| stays within a few ulp of hi); a sum is normalised once,
+// with a two-sum, when it is complete.
+__device__ __forceinline__ Df df_acc(Df a, Df t) {
+    const float s = a.hi + t.hi;
+    const float bb = s - a.hi;
+    const float e = (a.hi - (s - bb)) + (t.hi - bb);
+    return Df{s, a.lo + (t.lo + e)};
+}
+__device__ __forceinline__ Df df_mul_u(Df a, Df b) {
+    const float p = a.hi * b.hi;
+    float e = fmaf(a.hi, b.hi, -p);
+    e = fmaf(a.hi, b.lo, e);
+    e = fmaf(a.lo, b.hi, e);
+    return Df{p, e};
+}
+__device__ __forceinline__ Df df_mul_fu(Df a, float b) {
+    const float p = a.hi * b;
+    float e = fmaf(a.hi, b, -p);
+    e = fmaf(a.lo, b, e);
+    return Df{p, e};
+}
+__device__ __forceinline__ Df df_norm(Df a) { return df_two_sum(a.hi, a.lo); }
+
 // times a method coefficient: exact for +-1, +-2, +-4, +-1/2, else a double-float product
 __device__ __forceinline__ Df df_times_coef(Df a, double c) {
     if (c == 1.0) return a;
     if (c == -1.0 || c == 2.0 || c == -2.0 || c == 4.0 || c == -4.0 || c == 0.5 || c == -0.5) return df_scale(a, (float)c);
     return df_mul(a, df_from(c));
 }
+__device__ __forceinline__ Df df_times_coef_u(Df a, double c) {
+    if (c == 1.0) return a;
+    if (c == -1.0 || c == 2.0 || c == -2.0 || c == 4.0 || c == -4.0 || c == 0.5 || c == -0.5) return df_scale(a, (float)c);
+    return df_mul_u(a, df_from(c));
+}
 
-template <class Ops, class M>
+// kLuStride > 0: the FP32 LU lives in shared memory, interleaved across the CTA's lanes
+// (element e of lane t at [e * kLuStride + t]), which frees registers for the double-float vectors.
+template <class Ops, class M, int kLuStride = 0>
 struct LaneIr {
     static constexpr int N = Ops::N, R = Ops::R, NNZ = Ops::NNZ, S = M::kStages;
-    static constexpr size_t kSmemBytes = 0;
+    static constexpr size_t kSmemBytes = kLuStride ? (size_t)NNZ * kLuStride * sizeof(float) : 0;
 
     Ops ops;
     float yhi[N], ylo[N];
@@ -943,12 +976,19 @@ struct LaneIr {
     uint32_t iterations, transitions, attempts;
     int phase;
     bool pending, reject_last, reject_more;
-    float lu[NNZ];
-    float Yhi[N], Ylo[N], fhi[N], flo[N], bhi[N], blo[N], vhi[N], vlo[N];
+    float lu_r[kLuStride ? 1 : NNZ];
+    float *lu_s;
+    float Yhi[N], Ylo[N], fhi[N], flo[N], bhi[N], blo[N];
     float Khi[S][N], Klo[S][N];
     float x[N], x2[N];
 
-    __device__ __forceinline__ void bind(unsigned char *) {}
+    __device__ __forceinline__ void bind(unsigned char *smem) {
+        if constexpr (kLuStride > 0) lu_s = (float *)smem + threadIdx.x;
+    }
+    __device__ __forceinline__ void lu_solve(float *v) {
+        if constexpr (kLuStride > 0) ops.template solve<kLuStride>(lu_s, v);
+        else ops.solve(lu_r, v);
+    }
     __device__ __forceinline__ uint32_t n() const { return ops.n(); }
 
     __device__ __forceinline__ void load(const DevArgs &A, uint32_t i) {
@@ -1026,7 +1066,7 @@ struct LaneIr {
         phase = done ? kPhaseDone : kPhaseSegStart;
     }
 
-    __device__ __forceinline__ bool settle(const DevArgs &A, uint32_t) {
+    __device__ __forceinline__ bool settle(const DevArgs &A, uint32_t cell) {
         for (;;) {
             if (++transitions > (1u << 24)) {
                 failed = 1.0;
@@ -1034,7 +1074,7 @@ struct LaneIr {
             }
             switch (phase) {
                 case kPhaseSegStart: seg_start(A); break;
-                case kPhaseSegFinish: seg_finish(A, 0); break;
+                case kPhaseSegFinish: seg_finish(A, cell); break;
                 case kPhaseStepping:
                     ++attempts;
                     if (++iterations > A.ctl.max_steps) {
@@ -1060,9 +1100,16 @@ struct LaneIr {
         const double ghinv = 1.0 / (hs * M::gamma0(A)), hinv = 1.0 / hs;
         const Df gd = df_from(ghinv);
 
-        ops.neg_jac(khi, yhi, lu);   // FP32 -J at the FP32 rounding of y
-        if constexpr (kSync) __syncthreads();
-        ops.factor((float)ghinv, lu);
+        // FP32 -J at the FP32 rounding of y, factorised
+        if constexpr (kLuStride > 0) {
+            ops.template neg_jac<kLuStride>(khi, yhi, lu_s);
+            if constexpr (kSync) __syncthreads();
+            ops.template factor<kLuStride>((float)ghinv, lu_s);
+        } else {
+            ops.neg_jac(khi, yhi, lu_r);
+            if constexpr (kSync) __syncthreads();
+            ops.factor((float)ghinv, lu_r);
+        }
         if constexpr (kSync) __syncthreads();
 
         bool f_at_y = false;   // f (fhi, flo) holds f(y)
@@ -1086,13 +1133,21 @@ struct LaneIr {
                     moved = true;
                     for (int s = 0; s < N; ++s) {
                         if (s >= (int)nn) break;
-                        const Df v = df_add(Df{Yhi[s], Ylo[s]}, df_times_coef(Df{Khi[j][s], Klo[j][s]}, a));
+                        const Df v = df_acc(Df{Yhi[s], Ylo[s]}, df_times_coef_u(Df{Khi[j][s], Klo[j][s]}, a));
+                        Yhi[s] = v.hi;
+                        Ylo[s] = v.lo;
+                    }
+                }
+                if (moved) {
+                    for (int s = 0; s < N; ++s) {
+                        if (s >= (int)nn) break;
+                        const Df v = df_norm(Df{Yhi[s], Ylo[s]});
                         Yhi[s] = v.hi;
                         Ylo[s] = v.lo;
                     }
                 }
                 if (moved || !f_at_y) {
-                    ops.fun_df(khi, klo, shi, slo, Yhi, Ylo, fhi, flo);
+                    ops.fun_dfl(khi, klo, shi, slo, Yhi, Ylo, fhi, flo);
                     f_at_y = !moved;
                 }
             }
@@ -1110,23 +1165,22 @@ struct LaneIr {
                 const Df ch = df_from(c * hinv);
                 for (int s = 0; s < N; ++s) {
                     if (s >= (int)nn) break;
-                    const Df v = df_add(Df{bhi[s], blo[s]}, df_mul(ch, Df{Khi[j][s], Klo[j][s]}));
+                    const Df v = df_acc(Df{bhi[s], blo[s]}, df_mul_u(ch, Df{Khi[j][s], Klo[j][s]}));
                     bhi[s] = v.hi;
                     blo[s] = v.lo;
                 }
             }
             for (int s = 0; s < N; ++s) {
                 if (s >= (int)nn) break;
-                x[s] = bhi[s];
+                const Df v = df_norm(Df{bhi[s], blo[s]});
+                bhi[s] = v.hi;
+                blo[s] = v.lo;
+                x[s] = v.hi;
             }
-            ops.solve(lu, x);
+            lu_solve(x);
             // one refinement sweep: r = b - ghinv x + J x (double-float), x2 = W32^-1 r
-            ops.jvp_df(khi, klo, yhi, ylo, x, vhi, vlo);
-            for (int s = 0; s < N; ++s) {
-                if (s >= (int)nn) break;
-                x2[s] = df_add(df_add(Df{bhi[s], blo[s]}, df_neg(df_mul_f(gd, x[s]))), Df{vhi[s], vlo[s]}).hi;
-            }
-            ops.solve(lu, x2);
+            ops.residual_df(khi, klo, yhi, ylo, x, bhi, blo, gd, x2);
+            lu_solve(x2);
             for (int s = 0; s < N; ++s) {
                 if (s >= (int)nn) break;
                 const Df v = df_two_sum(x[s], x2[s]);
@@ -1148,12 +1202,14 @@ struct LaneIr {
                 if (st >= M::stages(A)) break;
                 const double mc = M::m(A, st), ec = M::e(A, st);
                 const Df kv{Khi[st][s], Klo[st][s]};
-                if (mc != 0.0) yn = df_add(yn, df_times_coef(kv, mc));
+                if (mc != 0.0) yn = df_acc(yn, df_times_coef_u(kv, mc));
                 if (ec != 0.0) {
-                    ye = first_e ? df_times_coef(kv, ec) : df_add(ye, df_times_coef(kv, ec));
+                    ye = first_e ? df_times_coef_u(kv, ec) : df_acc(ye, df_times_coef_u(kv, ec));
                     first_e = false;
                 }
             }
+            yn = df_norm(yn);
+            ye = df_norm(ye);
             const Df ay = df_abs(Df{yhi[s], ylo[s]}), an = df_abs(yn);
             const Df scale = df_add(df_mul(rtol, df_less(ay, an) ? an : ay), atol);
             const float inv = 1.0f / scale.hi;
@@ -1234,9 +1290,13 @@ struct GenOps {
         G::fun_df(khi, klo, shi, slo, yhi, ylo, fhi, flo);
     }
     __device__ SGB_OPS_QUALIFIER void fun_delta(const float *k, const float *y, const float *d, float *df) const { G::fun_delta(k, y, d, df); }
-    __device__ SGB_OPS_QUALIFIER void jvp_df(const float *khi, const float *klo, const float *yhi, const float *ylo, const float *x,
-                                             float *vhi, float *vlo) const {
-        G::jvp_df(khi, klo, yhi, ylo, x, vhi, vlo);
+    __device__ SGB_OPS_QUALIFIER void fun_dfl(const float *khi, const float *klo, const float *shi, const float *slo, const float *yhi,
+                                              const float *ylo, float *fhi, float *flo) const {
+        G::fun_dfl(khi, klo, shi, slo, yhi, ylo, fhi, flo);
+    }
+    __device__ SGB_OPS_QUALIFIER void residual_df(const float *khi, const float *klo, const float *yhi, const float *ylo, const float *x,
+                                                  const float *bhi, const float *blo, Df g, float *r) const {
+        G::residual_df(khi, klo, yhi, ylo, x, bhi, blo, g, r);
     }
     __device__ SGB_OPS_QUALIFIER void save_jac(const float *a, double *js) const { G::save_jac(a, js); }
     __device__ SGB_OPS_QUALIFIER void residual(const double *js, double ghinv, const double *b, const double *x, double *r) const {

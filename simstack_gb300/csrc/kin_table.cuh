@@ -135,36 +135,69 @@ struct TableOps {
         }
     }
 
-    // v = J(y) x in double-float in the generated code's order (kin_codegen.cpp, jvp_df).
-    __device__ __forceinline__ void jvp_df(const float *khi, const float *klo, const float *yhi, const float *ylo, const float *x,
-                                           float *vhi, float *vlo) const {
+    // acc += c * v, lazily normalised (kin_codegen.cpp, emit_lazy_term)
+    __device__ __forceinline__ static Df lazy_term(Df acc, Df v, int c) {
+        if (c == 1) return df_acc(acc, v);
+        if (c == -1 || c == 2 || c == -2 || c == 4 || c == -4) return df_acc(acc, df_scale(v, (float)c));
+        return df_acc(acc, df_mul_u(v, Df{(float)c, 0.0f}));
+    }
+
+    // f(y) in lazily normalised double-float in the generated code's order (kin_codegen.cpp, fun_dfl).
+    __device__ __forceinline__ void fun_dfl(const float *khi, const float *klo, const float *shi, const float *slo, const float *yhi,
+                                            const float *ylo, float *fhi, float *flo) const {
         const uint32_t ns = m->species_count, nr = m->reaction_count;
         for (uint32_t s = 0; s < ns; ++s) {
-            vhi[s] = 0.0f;
-            vlo[s] = 0.0f;
+            fhi[s] = shi[s];
+            flo[s] = slo[s];
         }
         for (uint32_t r = 0; r < nr; ++r) {
             const KinReaction &rx = m->reactions[r];
+            Df rate{khi[r], klo[r]};
+            for (uint32_t p = 0; p < rx.reactant_count; ++p) rate = df_mul_u(rate, Df{yhi[rx.reactant[p]], ylo[rx.reactant[p]]});
+            for (uint32_t e = 0; e < rx.net_count; ++e) {
+                const uint32_t s = rx.net_species[e];
+                const Df acc = lazy_term(Df{fhi[s], flo[s]}, rate, rx.net_coef[e]);
+                fhi[s] = acc.hi;
+                flo[s] = acc.lo;
+            }
+        }
+        for (uint32_t s = 0; s < ns; ++s) {
+            const Df v = df_norm(Df{fhi[s], flo[s]});
+            fhi[s] = v.hi;
+            flo[s] = v.lo;
+        }
+    }
+
+    // r = b - ghinv x + J(y) x in lazily normalised double-float, out as FP32, in the generated
+    // code's order (kin_codegen.cpp, residual_df).
+    __device__ __forceinline__ void residual_df(const float *khi, const float *klo, const float *yhi, const float *ylo, const float *x,
+                                                const float *bhi, const float *blo, Df g, float *r) const {
+        const uint32_t ns = m->species_count, nr = m->reaction_count;
+        float ahi[KIN_MAX_SPECIES], alo[KIN_MAX_SPECIES];
+        for (uint32_t s = 0; s < ns; ++s) {
+            const Df a = df_acc(Df{bhi[s], blo[s]}, df_neg(df_mul_fu(g, x[s])));
+            ahi[s] = a.hi;
+            alo[s] = a.lo;
+        }
+        for (uint32_t q = 0; q < nr; ++q) {
+            const KinReaction &rx = m->reactions[q];
             if (rx.reactant_count == 0) continue;
             Df drate{0.0f, 0.0f};
             for (uint32_t p = 0; p < rx.reactant_count; ++p) {
-                Df t{khi[r], klo[r]};
-                for (uint32_t q = 0; q < rx.reactant_count; ++q)
-                    if (q != p) t = df_mul(t, Df{yhi[rx.reactant[q]], ylo[rx.reactant[q]]});
-                t = df_mul_f(t, x[rx.reactant[p]]);
-                drate = p == 0 ? t : df_add(drate, t);
+                Df t{khi[q], klo[q]};
+                for (uint32_t o = 0; o < rx.reactant_count; ++o)
+                    if (o != p) t = df_mul_u(t, Df{yhi[rx.reactant[o]], ylo[rx.reactant[o]]});
+                t = df_mul_fu(t, x[rx.reactant[p]]);
+                drate = p == 0 ? t : df_acc(drate, t);
             }
             for (uint32_t e = 0; e < rx.net_count; ++e) {
                 const uint32_t s = rx.net_species[e];
-                const int c = rx.net_coef[e];
-                Df term = c == 1 ? drate
-                          : (c == -1 || c == 2 || c == -2 || c == 4 || c == -4) ? df_scale(drate, (float)c)
-                                                                                 : df_mul(drate, Df{(float)c, 0.0f});
-                const Df acc = df_add(Df{vhi[s], vlo[s]}, term);
-                vhi[s] = acc.hi;
-                vlo[s] = acc.lo;
+                const Df a = lazy_term(Df{ahi[s], alo[s]}, drate, rx.net_coef[e]);
+                ahi[s] = a.hi;
+                alo[s] = a.lo;
             }
         }
+        for (uint32_t s = 0; s < ns; ++s) r[s] = ahi[s] + alo[s];
     }
 
     __device__ __forceinline__ bool in_jac(uint32_t slot) const {

@@ -30,7 +30,7 @@ def test_defaults_are_the_headline(monkeypatch):
 
 def test_runners_exist():
     for name in ("run_ours", "run_reference", "run_uneven_stiffness", "run_large_mechanism", "run_serving",
-                 "run_profile_case"):
+                 "run_profile_case", "run_dbd_sweep"):
         assert callable(getattr(bench, name))
 
 
@@ -38,9 +38,18 @@ def test_algorithmic_counts_of_the_shipped_mechanism():
     import simstack_gb300 as sg
 
     f = bench.flops_per_step(sg.Model.air())
-    assert f["total"] == 6032
+    assert f["total"] == 6032 and f["executed_f64"] == 5639   # the FP64 path reuses f(y) at Rodas3's stage 2
     assert (f["fun"], f["neg_jac"], f["factor"], f["solve"]) == (393, 694, 1552, 409)
     assert bench.hbm_bytes_per_cell(17, 44) == 808
+
+
+def test_mixed_error_definition():
+    """Every entry counts; relative to max(|b|, atol); the filtered figure is reported beside it."""
+    b = np.array([[1e12, 1e12], [1e3, 1e3]])
+    a = b.copy()
+    a[1, 0] += 6.02214076e8 * 1e-6   # a tiny species off by 1e-6 atol
+    e = bench.mixed_errors(a, b)
+    assert abs(e["max"] - 1e-6) < 1e-12 and e["max_species_above_1e-3_ppm"] == 0.0
 
 
 def test_served_stream_is_seeded_and_in_range():
