@@ -206,13 +206,14 @@ FP64_FMA_PER_CLK_SM = 2      # GB300: FP64 FMAs per clock per SM
 FP32_LANES_SM = 128          # FP32 lanes per SM
 
 
-# DRAM bytes (read + write) per attempted cell-step of the queue kernels, from one ncu capture each
-# (262,144 cells x 0.5 s, `bench.py --profile-case f64|mixed`; FP64 with the default tuning, mixed with the
-# shape the autotuner picks for the benchmark, 256 threads x 1 CTA/SM; summaries in
-# profiles/kin_queue_cta_f64_air_262144x0.5s.txt and profiles/kin_queue_cta_mixed_df_256thr_air_262144x0.5s.txt).
-# Nearly all of it is local-memory spill traffic, which grows with the cell-steps a launch executes;
-# the bench scales it to its own launch.
-DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 2045.3}
+# Per attempted cell-step of the queue kernels, from one ncu capture each (262,144 cells x 0.5 s,
+# `bench.py --profile-case f64|mixed`, the benchmark's launch shapes; summaries in profiles/):
+# DRAM bytes read + written -- local-memory traffic, which grows with the cell-steps a launch
+# executes, so the bench scales it to its own launch -- and, for the mixed lanes, the FP32 flops
+# executed (FADD + FMUL + 2 FFMA thread instructions; FP32 work per algorithmic flop is high
+# because the state, right-hand sides and residuals are double-float).
+DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 506.8}
+MIXED_FP32_FLOPS_PER_CELL_STEP = 31683.0
 PIPELINE_CHUNKS = (2, 4)   # lane-chunk counts tried for the pipelined end-to-end call (8 and 16 measured slower)
 
 
@@ -266,12 +267,13 @@ def cpu_kind() -> str:
     return "reference" if O.ref_available() else "port"
 
 
-def cpu_sample_cells(kind: str, cells_total: int, duration: float, seed: int, target_s: float, threads: int) -> int:
+def cpu_sample_cells(kind: str, cells_total: int, duration: float, seed: int, target_s: float, threads: int,
+                     source_P0: float = 0.0) -> int:
     """Cells (a multiple of 64) of the workload the CPU integrates in about target_s."""
     from oracle import oracle as O
 
     probe_cells = max(64, 8 * threads) // 8 * 8
-    block, P, _ = O.air_block(probe_cells, seed=seed)
+    block, P, _ = O.air_block(probe_cells, seed=seed, source_P0=source_P0)
     per_cell = _cpu_advance(kind, block, P, duration, threads) / probe_cells
     cells = int(min(cells_total, max(probe_cells, target_s / max(per_cell, 1e-9))))
     return max(64, cells // 64 * 64)
@@ -285,20 +287,21 @@ CPU_PATHS = {"reference": "the reference's dbd_advance_threads<f64x4, AirGenOps>
              "port": "oracle/kin_oracle.cpp, the reference's FP64 algorithm restated (bit-identical to its CPU path)"}
 
 
-def cpu_baseline(cells_total: int, duration: float, seed: int, target_s: float, with_port: bool = True):
+def cpu_baseline(cells_total: int, duration: float, seed: int, target_s: float, with_port: bool = True,
+                 source_P0: float = 0.0):
     from oracle import oracle as O
 
     kind = cpu_kind()
     threads = os.cpu_count() or 1
-    cells = cpu_sample_cells(kind, cells_total, duration, seed, target_s, threads)
-    block, P, rates = O.air_block(cells, seed=seed)
+    cells = cpu_sample_cells(kind, cells_total, duration, seed, target_s, threads, source_P0)
+    block, P, rates = O.air_block(cells, seed=seed, source_P0=source_P0)
     wall = _cpu_advance(kind, block, P, duration, threads)
     out = {"value": cells / wall, "unit": "cell-integrations/s", "cores": threads, "kind": kind,
            "sample": f"first {cells} cells of the workload (same seeded inputs), {duration:g} s each, {threads} host "
                      f"threads, {wall:.1f} s wall; {CPU_PATHS[kind]}; rate constants from the {rates}",
            "wall_s": wall, "cells": cells, "y": block["y"][:, :cells].copy()}
     if with_port and kind == "reference":   # the restatement on the same sample, for comparison
-        block, P, _ = O.air_block(cells, seed=seed)
+        block, P, _ = O.air_block(cells, seed=seed, source_P0=source_P0)
         wall_p = _cpu_advance("port", block, P, duration, threads)
         out["port"] = {"value": cells / wall_p, "kind": "port", "cores": threads, "sample": CPU_PATHS["port"]}
     return out
@@ -676,14 +679,22 @@ def run_uneven_stiffness(args):
             elif prec == 0:   # the hand-off keeps the FP64 bits
                 results[key]["same_bits_as_f64_static"] = bool(zo["y"].tobytes() == zf["y"].tobytes())
             else:
-                b, a = zf["y"][:, :cells], zo["y"][:, :cells]
-                sig = b >= 1e-12 * b.sum(axis=0)
-                with np.errstate(all="ignore"):
-                    rel = (np.abs(a - b) / np.abs(b))[sig]
-                results[key]["rel_err_vs_fp64"] = {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99))}
+                results[key]["rel_err_vs_fp64"] = mixed_errors(zo["y"][:, :cells], zf["y"][:, :cells])
     mod.set_straggler_budget(UNEVEN_HANDOFF_BUDGET)
     steps = zf["steps"][:cells]   # FP64 path: the oracle's step counts
+    attempts = float(zf["steps"][:cells].sum() + zf["rejects"][:cells].sum())
     best = min((k for k in results if k.startswith("mixed")), key=lambda k: results[k]["ms"])
+    sms = int(mod.info.multiprocessors)
+    clk_hz = 2070.0e6
+    fp32_peak = sms * FP32_LANES_SM * 2 * clk_hz / 1e12
+    fp64_peak = sms * FP64_FMA_PER_CLK_SM * 2 * clk_hz / 1e12
+    f_exec = flops_per_step(sg.Model.air())["executed_f64"]
+    cpu = None
+    if not args.no_cpu:
+        cpu = cpu_baseline(cells, duration, args.seed, args.cpu_seconds, with_port=False, source_P0=UNEVEN_SOURCE_P0)
+        m, ref_y = cpu.pop("cells"), cpu.pop("y")
+        cpu.pop("wall_s")
+        cpu["fp64_bit_identical_on_sample"] = bool(np.array_equal(zf["y"][:, :m], ref_y))
     line = {"metric": "cell-integrations/s", "value": results[best]["value"], "unit": "cell-integrations/s",
             "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": results[best]["ms"],
             "headline_kernel": best,
@@ -696,7 +707,18 @@ def run_uneven_stiffness(args):
             "kernels": results,
             "queue_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue"]["ms"],
                                         "mixed": results["mixed_static"]["ms"] / results["mixed_queue"]["ms"]},
-            "handoff_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue_handoff"]["ms"]}}
+            "handoff_speedup_vs_static": {"f64": results["f64_static"]["ms"] / results["f64_queue_handoff"]["ms"]},
+            "roofline": {"bound": "fp32", "unit": "TFLOP/s", "peak": fp32_peak,
+                         "achieved": MIXED_FP32_FLOPS_PER_CELL_STEP * attempts / (results[best]["ms"] * 1e-3) / 1e12,
+                         "frac": MIXED_FP32_FLOPS_PER_CELL_STEP * attempts / (results[best]["ms"] * 1e-3) / 1e12 / fp32_peak,
+                         "of": "152 SMs x 128 FP32 lanes x 2 x 2,070 MHz",
+                         "work": "FP32 flops executed per cell-step of the mixed lanes (ncu) x attempted cell-steps",
+                         "traffic": DRAM_BYTES_PER_CELL_STEP["mixed"] * attempts,
+                         "fp64_handoff": {"achieved": f_exec * attempts / (results["f64_queue_handoff"]["ms"] * 1e-3) / 1e12,
+                                          "peak": fp64_peak,
+                                          "frac": f_exec * attempts / (results["f64_queue_handoff"]["ms"] * 1e-3) / 1e12
+                                          / fp64_peak}},
+            "cpu_baseline": cpu}
     print(json.dumps(line))
 
 
@@ -855,10 +877,7 @@ def run_large_mechanism(args):
     clk = clocks.stop()
     zm = z.copy()
     mod.download(zm, base)
-    a, b = zm["y"][:, :nf], zf["y"][:, :nf]
-    sig = b >= 1e-9 * b.sum(axis=0)
-    with np.errstate(all="ignore"):
-        rel = (np.abs(a - b) / np.abs(b))[sig]
+    err = mixed_errors(zm["y"][:, :nf], zf["y"][:, :nf], atol=1e-12)
     steps64 = float(zf["steps"][:nf].sum() + zf["rejects"][:nf].sum())
     stepsmx = float(zm["steps"][:cells].sum() + zm["rejects"][:cells].sum())
     # algorithmic flops per Rodas3 step: LU 2 per update + 4 divisions, 4 solves over the L and U
@@ -869,6 +888,10 @@ def run_large_mechanism(args):
                   + 4 * (int(1.7 * R) + 2 * 2 * R) + 2 * 2 * info["jac_entries"] + 12 * n)
     dfma = mod.probe(0)
     ffma = mod.probe(1)
+    clk_hz = (clk.get("sm_mhz") or 2070.0) * 1e6
+    sms = int(mod.info.multiprocessors)
+    fp64_peak = sms * FP64_FMA_PER_CLK_SM * 2 * clk_hz   # flop/s
+    fp32_peak = sms * FP32_LANES_SM * 2 * clk_hz
     v64 = nf / (ms64 * 1e-3)
     vmx = cells / (msmx * 1e-3)
     # CPU: the oracle (the reference's algorithm with 32-bit indices) on a bounded sample, all host threads
@@ -896,17 +919,22 @@ def run_large_mechanism(args):
                      "parity": "bit-identical to the oracle (tests/test_gpu_coop.py) and to the reference's own "
                                "solver on a 60-species mechanism",
                      "achieved_tflops": steps64 * flops_step / (ms64 * 1e-3) / 1e12,
-                     "frac_of_fp64_peak": steps64 * flops_step / (ms64 * 1e-3) / (2 * dfma)},
+                     "frac_of_fp64_peak": steps64 * flops_step / (ms64 * 1e-3) / fp64_peak,
+                     "fp64_peak_tflops": fp64_peak / 1e12},
             "mixed": {"value": vmx, "kernel_ms": msmx, "speedup_vs_fp64": vmx / v64,
-                      "rel_err_vs_fp64": {"max": float(rel.max()), "p99": float(np.quantile(rel, 0.99)),
-                                          "cells": nf, "definition": "species >= 1e-9 of the cell total"},
+                      "rel_err_vs_fp64": dict(err, cells=nf, definition="|a-b| / max(|b|, atol) over every species of "
+                                                                        "the FP64 sample's cells, no filter"),
                       "achieved_tflops_fp64_equivalent": stepsmx * flops_step / (msmx * 1e-3) / 1e12,
-                      "frac_of_fp32_peak": stepsmx * flops_step / (msmx * 1e-3) / (2 * ffma)},
+                      "frac_of_fp32_peak": stepsmx * flops_step / (msmx * 1e-3) / fp32_peak},
             "steps_per_cell": {"fp64_mean": steps64 / nf, "mixed_mean": stepsmx / cells},
             "algorithmic_flops_per_step": flops_step,
             "roofline": {"bound": "fp32", "achieved": stepsmx * flops_step / (msmx * 1e-3) / 1e12,
-                         "peak": 2 * ffma / 1e12, "unit": "TFLOP/s",
-                         "frac": stepsmx * flops_step / (msmx * 1e-3) / (2 * ffma), "traffic": None},
+                         "peak": fp32_peak / 1e12, "unit": "TFLOP/s",
+                         "frac": stepsmx * flops_step / (msmx * 1e-3) / fp32_peak, "traffic": None,
+                         "of": "SMs x 128 FP32 lanes x 2 x the sampled SM clock",
+                         "probes": {"fp64_fma_tflops": 2 * dfma / 1e12, "fp32_fma_tflops": 2 * ffma / 1e12},
+                         "work": "algorithmic flops per Rodas3 step x attempted cell-steps (the FP32 LU's own flops "
+                                 "counted once)"},
             "cpu_baseline": {"value": ncpu / cpu_s, "unit": "cell-integrations/s", "cores": threads, "kind": "port",
                              "sample": f"first {ncpu} cells, {duration:g} s each, oracle/kin_oracle.cpp on {threads} "
                                        f"host threads ({cpu_s:.1f} s); same bits as the GPU FP64 path: {cpu_ok}"},
@@ -914,81 +942,143 @@ def run_large_mechanism(args):
     print(json.dumps(line))
 
 
-def serve_sample(seed: int, count: int, rate_hz: float = 200.0):
+# Requests on the 200-species synthetic mechanism cost about 100x more per cell-step than the
+# shipped one; in the served mix their size and horizon are capped at these values so that the
+# whole stream finishes in minutes (the cap is recorded in the JSON line).
+SERVE_MECH200_MAX_CELLS, SERVE_MECH200_MAX_STEPS = 2048, 2
+
+
+def serve_sample(seed: int, count: int, rate_hz: float = 200.0, mix: bool = True):
     """The served request stream: Poisson arrivals at rate_hz; cells 10^U[log10 1024, log10 65536];
     horizon 10^U[0, log10 600] s in 1 s coupling steps (log-uniform); channel cells U{256..4096};
-    film speed U[0.01, 0.1] m/s; dx = 0.05 m; shipped mechanism."""
+    film speed U[0.01, 0.1] m/s; dx = 0.05 m; mechanism: the shipped one or (mix, probability 1/2)
+    the 200-species synthetic one, whose requests are capped at SERVE_MECH200_MAX_CELLS cells and
+    SERVE_MECH200_MAX_STEPS steps."""
     rng = np.random.default_rng(seed)
     t = np.cumsum(rng.exponential(1.0 / rate_hz, size=count))
     cells = np.rint(10.0 ** rng.uniform(np.log10(1024), np.log10(65536), size=count)).astype(int)
     horizon = np.maximum(1, np.rint(10.0 ** rng.uniform(0.0, np.log10(600.0), size=count))).astype(int)
     channel = rng.integers(256, 4097, size=count)
     v = rng.uniform(0.01, 0.1, size=count)
-    return [dict(arrival_s=float(t[i]), cells=int(cells[i]), steps=int(horizon[i]), channel_cells=int(channel[i]),
-                 velocity=float(v[i]), seed=seed * 1000 + i) for i in range(count)]
+    big = rng.uniform(size=count) < 0.5 if mix else np.zeros(count, bool)
+    out = []
+    for i in range(count):
+        c, h = int(cells[i]), int(horizon[i])
+        if big[i]:
+            c, h = min(c, SERVE_MECH200_MAX_CELLS), min(h, SERVE_MECH200_MAX_STEPS)
+        out.append(dict(arrival_s=float(t[i]), cells=c, steps=h, channel_cells=int(channel[i]), velocity=float(v[i]),
+                        seed=seed * 1000 + i, mechanism=2 if big[i] else 0))
+    return out
+
+
+def _serve_stream(sg, reqs, inputs, prec, budget_bytes=0, big_model=None):
+    """Submits every request at its arrival time and drives the engine until all are done."""
+    with sg.Server(budget_bytes) as srv:
+        if big_model is not None:
+            srv.set_coop_mech(big_model)
+        srv.submit(inputs[0][0][:, :1024], inputs[0][1][:, :1024], 1, 256, 0.05, precision=prec,
+                   mechanism=reqs[0]["mechanism"])   # warm-up: kernels loaded, pools primed
+        srv.drain(timeout_s=300)
+        ids = [None] * len(reqs)
+        nxt = 0
+        t0 = time.monotonic()
+        while True:
+            now = time.monotonic() - t0
+            while nxt < len(reqs) and reqs[nxt]["arrival_s"] <= now:
+                r = reqs[nxt]
+                ids[nxt] = srv.submit(inputs[nxt][0], inputs[nxt][1], r["steps"], r["channel_cells"], r["velocity"],
+                                      precision=prec, mechanism=r["mechanism"])
+                nxt += 1
+            running, waiting, _ = srv.progress()
+            if nxt == len(reqs) and running == 0 and waiting == 0:
+                break
+            time.sleep(1e-4)
+        makespan = time.monotonic() - t0
+        polls = [srv.poll(i) for i in ids]
+        results = [srv.result(i) for i in ids]
+        st = srv.stats()
+    lat = np.array([p["latency_s"] for p in polls])
+    admit = np.array([p["admit_s"] for p in polls])
+    attempts = {0: 0.0, 2: 0.0}
+    for r, (y, steps, failed) in zip(reqs, results):
+        attempts[r["mechanism"]] += float(steps.sum())
+    return {"makespan_s": makespan, "lat": lat, "admit": admit, "states": sorted({p["state"] for p in polls}),
+            "failed_cells": int(sum(res[2].sum() for res in results)), "stats": st, "accepted_steps": attempts}
 
 
 def run_serving(args):
     """Serving: requests submitted at their arrival times through the public serving API
-    (host arrays in, results back on the host), the engine driven until every request is done."""
-    import time
-
+    (host arrays in, results back on the host), the engine driven until every request is done;
+    a 50/50 mix of the shipped and the 200-species mechanism; then the same stream under an HBM
+    budget below its summed footprint, so that admission gates."""
     import simstack_gb300 as sg
 
     reqs = serve_sample(args.seed, args.requests)
+    big = sg.Model.synthetic(seed=args.seed, species=200, reactions=1200, bimolecular=0.7, products=1)
     inputs = []
     for r in reqs:
-        z = sg.air_cells(r["cells"], seed=r["seed"])
+        if r["mechanism"] == 0:
+            z = sg.air_cells(r["cells"], seed=r["seed"])
+        else:
+            z = sg.synthetic_cells(big, r["cells"], seed=r["seed"])
         inputs.append((np.ascontiguousarray(z["y"][:, :r["cells"]]), np.ascontiguousarray(z["k"][:, :r["cells"]])))
-    out = {}
     clocks = ClockSampler(0)
-    clock_summary = None
+    out, clock_summary = {}, None
+    cell_steps = sum(r["cells"] * r["steps"] for r in reqs)
     for prec, name in ((0, "f64"), (2, "mixed")):
-        with sg.Server() as srv:
-            # warm-up: one small request through the same path (kernel loading, pools)
-            srv.submit(inputs[0][0][:, :1024], inputs[0][1][:, :1024], 1, 256, 0.05, precision=prec)
-            srv.drain(timeout_s=120)
-            ids = [None] * len(reqs)
-            nxt = 0
-            if name == "mixed":
-                clocks.start()
-            t0 = time.monotonic()
-            while True:
-                now = time.monotonic() - t0
-                while nxt < len(reqs) and reqs[nxt]["arrival_s"] <= now:
-                    r = reqs[nxt]
-                    ids[nxt] = srv.submit(inputs[nxt][0], inputs[nxt][1], r["steps"], r["channel_cells"], r["velocity"],
-                                          precision=prec)
-                    nxt += 1
-                running, waiting, _ = srv.progress()
-                if nxt == len(reqs) and running == 0 and waiting == 0:
-                    break
-                time.sleep(1e-4)
-            makespan = time.monotonic() - t0
-            if name == "mixed":
-                clock_summary = clocks.stop()
-            lat = np.array([srv.poll(i)["latency_s"] for i in ids])
-            states = {srv.poll(i)["state"] for i in ids}
-            failed = sum(int(srv.result(i)[2].sum()) for i in ids)
-            st = srv.stats()
-        cell_steps = sum(r["cells"] * r["steps"] for r in reqs)
-        out[name] = {"makespan_s": makespan, "cell_steps_per_s": cell_steps / makespan,
-                     "cell_integrations_per_s": sum(r["cells"] for r in reqs) / makespan,
-                     "latency_s": {"p50": float(np.median(lat)), "p99": float(np.quantile(lat, 0.99)),
-                                   "max": float(lat.max())},
-                     "states": sorted(states), "failed_cells": failed, "graph_launches": st["graph_launches"] - 1,
-                     "peak_device_bytes": st["peak_bytes"]}
+        if name == "mixed":
+            clocks.start()
+        res = _serve_stream(sg, reqs, inputs, prec, big_model=big)
+        if name == "mixed":
+            clock_summary = clocks.stop()
+        out[name] = {"makespan_s": res["makespan_s"], "cell_steps_per_s": cell_steps / res["makespan_s"],
+                     "cell_integrations_per_s": sum(r["cells"] for r in reqs) / res["makespan_s"],
+                     "latency_s": {"p50": float(np.median(res["lat"])), "p99": float(np.quantile(res["lat"], 0.99)),
+                                   "max": float(res["lat"].max())},
+                     "states": res["states"], "failed_cells": res["failed_cells"],
+                     "graph_launches": res["stats"]["graph_launches"] - 1, "peak_device_bytes": res["stats"]["peak_bytes"],
+                     "accepted_rodas3_steps": res["accepted_steps"]}
+    # admission that gates: a budget of a quarter of the stream's peak footprint
+    peak = out["mixed"]["peak_device_bytes"]
+    gated = _serve_stream(sg, reqs, inputs, 2, budget_bytes=max(peak // 4, 64 << 20), big_model=big)
+    out["mixed_gated"] = {"budget_bytes": gated["stats"]["budget_bytes"], "peak_device_bytes": gated["stats"]["peak_bytes"],
+                          "requests_that_waited": int(np.sum(gated["admit"] > 1e-3)),
+                          "makespan_s": gated["makespan_s"],
+                          "latency_s": {"p50": float(np.median(gated["lat"])), "p99": float(np.quantile(gated["lat"], 0.99))},
+                          "states": gated["states"]}
     m = out["mixed"]
+    # roofline of the chemistry inside the stream: the shipped mechanism's accepted Rodas3 steps (a lower bound of
+    # the attempts) x the mixed lanes' executed FP32 flops per step, over the makespan
+    sms, clk_hz = 152, (clock_summary or {}).get("sm_mhz") or 2070.0
+    fp32_peak = sms * FP32_LANES_SM * 2 * clk_hz * 1e6 / 1e12
+    ach = MIXED_FP32_FLOPS_PER_CELL_STEP * m["accepted_rodas3_steps"][0] / m["makespan_s"] / 1e12
+    cpu = None
+    if not args.no_cpu:   # the reference's CPU solver on shipped-mechanism cells, one 1 s coupling step each
+        cpu = cpu_baseline(1 << 16, 1.0, args.seed, args.cpu_seconds, with_port=False)
+        for key in ("cells", "wall_s", "y"):
+            cpu.pop(key)
+        cpu["unit"] = "cell-steps/s"
+        cpu["sample"] += "; chemistry only (no advection): cell-steps of the shipped mechanism"
     line = {"metric": "served cell-steps/s (1 s coupling steps)", "value": m["cell_steps_per_s"],
             "unit": "cell-steps/s", "n_gpus": 1, "steps": 1, "warmup": 1, "ms_per_step": m["makespan_s"] * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {"workload": f"serving: {len(reqs)} requests, Poisson arrivals at 200 req/s (seed {args.seed}), "
                                    "cells 10^U[log10 1024, log10 65536], horizon 10^U[0, log10 600] s (log-uniform), "
-                                   "channel cells U{256..4096}, v U[0.01, 0.1] m/s, dx 0.05 m, shipped mechanism",
-                       "cell_steps": cell_steps, "requests": len(reqs)},
+                                   "channel cells U{256..4096}, v U[0.01, 0.1] m/s, dx 0.05 m; mechanism 50/50 the "
+                                   "shipped one or the 200-species synthetic one, the latter capped at "
+                                   f"{SERVE_MECH200_MAX_CELLS} cells and {SERVE_MECH200_MAX_STEPS} steps",
+                       "cell_steps": cell_steps, "requests": len(reqs),
+                       "mechanism200_requests": sum(r["mechanism"] == 2 for r in reqs)},
             "e2e": {"value": m["cell_steps_per_s"], "unit": "cell-steps/s",
-                    "h2d_bytes_per_step": sum(8 * (3 * 17 + 44 + 8) * ((r["cells"] + 7) // 8 * 8) for r in reqs),
-                    "d2h_bytes_per_step": sum(8 * (17 + 5) * ((r["cells"] + 7) // 8 * 8) for r in reqs)},
+                    "h2d_bytes_per_step": sum(8 * (3 * inp[0].shape[0] + inp[1].shape[0] + 8) * ((r["cells"] + 7) // 8 * 8)
+                                              for r, inp in zip(reqs, inputs)),
+                    "d2h_bytes_per_step": sum(8 * (inp[0].shape[0] + 5) * ((r["cells"] + 7) // 8 * 8)
+                                              for r, inp in zip(reqs, inputs))},
+            "roofline": {"bound": "fp32", "achieved": ach, "peak": fp32_peak, "unit": "TFLOP/s", "frac": ach / fp32_peak,
+                         "work": "shipped-mechanism requests' accepted Rodas3 steps x FP32 flops per step of the mixed "
+                                 "lanes, over the makespan (host submission and the 200-species requests included in "
+                                 "the time)", "traffic": None},
+            "cpu_baseline": cpu,
             "gpu_launches": 2 * m["graph_launches"], "clocks": clock_summary, "precisions": out,
             "mixed_speedup_vs_f64": out["f64"]["makespan_s"] / m["makespan_s"]}
     print(json.dumps(line))

@@ -180,7 +180,8 @@ SGB_API int32_t gpu_kin_advance_async(const GpuKinLaunch *launch, void *host_blo
                                       uint64_t mutable_rows);
 /* gpu_api.h:105 */
 SGB_API int32_t gpu_kin_wait(float *kernel_ms, float *total_ms);
-/* gpu_api.h:109 -- 0 = one thread per cell, 1 = one warp per cell. */
+/* gpu_api.h:109 -- 0 = one thread per cell, 1 = one warp per cell (FP64 and mixed advances run the
+ * cooperative kernel with 32 threads per cell; FP64 keeps the same bits). */
 SGB_API int32_t gpu_kin_set_mode(uint32_t mode);
 
 /* --------------------------------------------------------------------------
@@ -202,14 +203,19 @@ SGB_API int32_t gpu_kin_advance_pipelined(const GpuKinLaunch *launch, void *host
 
 /* Launch tuning. kind: 0 static one-cell-per-thread, 1 persistent queue
  * (warp-synchronous), 2 persistent queue with the CTA's warps stepping
- * together (default). block = threads per CTA (multiple of 32; <= 128, 256
- * with variant 2, 512 with variant 3), chunk = resident CTAs per SM for the
- * queue kernels (0: as many as fit), variant = compiled register-budget
- * variant (0: up to 255 registers at 128 threads, 1: 128 registers, 2: 255
- * registers at 256 threads, kind 2 only; 3: 128 registers at 512 threads,
- * kind 2 only).
- * gpu_kin_autotune times candidates on the given launch (which it advances
- * repeatedly on a scratch copy it restores) and keeps the fastest. */
+ * together (default), 3 cooperative: one cell per CTA of `block` threads
+ * (32 = one warp per cell; 64..256 = 1/2..1/8 of a cell per warp; FP64 and
+ * mixed only; FP64 gives the same bits as kinds 0-2). For kinds 0-2, block =
+ * threads per CTA (multiple of 32; <= 128, 256 with variant 2, 512 with
+ * variant 3), chunk = resident CTAs per SM for the queue kernels (0: as many
+ * as fit), variant = compiled register-budget variant (0: up to 255 registers
+ * at 128 threads, 1: 128 registers, 2: 255 registers at 256 threads, kind 2
+ * only; 3: 128 registers at 512 threads, kind 2 only); for kind 3, chunk =
+ * CTAs per SM (1..8, 0 = 8).
+ * gpu_kin_autotune times the candidates of `kind` on the given launch (which
+ * it advances repeatedly on a scratch copy it restores) and keeps the fastest;
+ * kind 4 times kinds 2 and 3 together, so the cells-per-warp decomposition is
+ * chosen by measurement as well. */
 typedef struct GpuKinTuning {
     uint32_t kind, block, chunk, variant;
     float ms;

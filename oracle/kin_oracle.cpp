@@ -1689,6 +1689,11 @@ static inline u64 wl_mix64(u64 z) {
 static inline double wl_uniform(u64 seed, u64 cell, u32 j) {
     return (double)(wl_mix64(seed + (cell * 256ull + j + 1ull) * 0x9E3779B97F4A7C15ull) >> 11) * (1.0 / 9007199254740992.0);
 }
+// The uneven-stiffness workload's discharge power per cell: P0 x 10^(decades x draw 250).
+void or_workload_air_power(u64 seed, u64 first_cell, u32 cells, double P0, double decades, double *power) {
+    for (u32 i = 0; i < cells; ++i) power[i] = P0 * std::pow(10.0, decades * wl_uniform(seed, first_cell + i, 250));
+}
+
 void or_workload_air(u64 seed, u64 first_cell, u32 cells, u32 padded, u32 n, double T_lo, double T_hi, double lc_lo,
                      double lc_hi, double *y, double *T_out, double *M_out) {
     for (u32 i = 0; i < cells; ++i) {

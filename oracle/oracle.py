@@ -120,6 +120,7 @@ def lib() -> C.CDLL:
         L.or_fnv1a.restype = u64
         L.or_rate_block.argtypes = [vp, vp, vp, u32, u32, vp]
         L.or_workload_air.argtypes = [u64, u64, u32, u32, u32, d, d, d, d, vp, vp, vp]
+        L.or_workload_air_power.argtypes = [u64, u64, u32, d, d, vp]
         _lib = L
     return _lib
 
@@ -252,7 +253,7 @@ def advect(x: np.ndarray, inlet: np.ndarray, courant: float, substeps: int) -> N
 
 
 def air_block(cells: int, seed: int = 1, first_cell: int = 0, pad_to: int = 8, T=(288.0, 303.0),
-              log10_c=(-12.0, -2.0), rates: str = "reference"):
+              log10_c=(-12.0, -2.0), rates: str = "reference", source_P0: float = 0.0, source_decades: float = 3.0):
     """The shipped-mechanism workload as a zone block (dict of 64-byte aligned float64 rows,
     `padded` lanes), built without the GPU module: the same seeded draws as the module's
     workload generator, rate constants from the reference's own kin_eval_rate_constants
@@ -276,6 +277,14 @@ def air_block(cells: int, seed: int = 1, first_cell: int = 0, pad_to: int = 8, T
     for i in range(cells, P):
         block["y"][:, i] = block["y"][:, 0]
         block["k"][:, i] = block["k"][:, 0]
+        T_v[i] = T_v[0]
+    if source_P0 > 0.0:   # the uneven-stiffness workload's averaged discharge source per second, every lane
+        power = np.zeros(P)
+        lib().or_workload_air_power(seed, first_cell, P, source_P0, source_decades, _ptr(power))
+        for i in range(P):
+            col = np.ascontiguousarray(block["y"][:, i])
+            block["src"][:, i] = (ref_air_source_delta(col, power[i], T_v[i]) if used == "reference"
+                                  else source_delta(col, power[i], T_v[i]))
     return block, P, used
 
 

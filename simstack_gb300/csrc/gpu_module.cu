@@ -163,6 +163,10 @@ cudaError_t launch_lanes(uint32_t prec, const GpuKinTuning &t, const DevArgs &A,
 
 // Local memory per thread the kernel of (precision, tuning) needs.
 cudaError_t local_bytes(uint32_t prec, const GpuKinTuning &t, size_t *bytes) {
+    if (t.kind == 3) {   // the cooperative kernel keeps its state in shared and global memory
+        *bytes = 0;
+        return cudaSuccess;
+    }
     const bool df = prec == 2 && g.mixed_variant == 1;
     if (prec == 2 && g.mixed_variant == 2) return g.generated ? local_air_p4(t.kind, t.variant, bytes) : local_table_p4(t.kind, bytes);
     if (g.generated) {
@@ -181,6 +185,20 @@ cudaError_t local_bytes(uint32_t prec, const GpuKinTuning &t, size_t *bytes) {
 // cooperative FP64 steps, so they keep their cells.)
 cudaError_t launch_advance(uint32_t prec, const GpuKinTuning &t, const DevArgs &A0) {
     if (A0.lanes == 0) return cudaSuccess;
+    if (t.kind == 3) {   // cooperative decomposition: one cell per CTA of t.block threads (32: one warp per cell)
+        if (!g.d_coop_image || prec == 1) return cudaErrorInvalidValue;
+        DevArgs R = A0;
+        R.budget = 0;
+        R.resume = 0;
+        R.tables = g.d_coop_image;
+        R.table_bytes = g.coop_head.bytes;
+        const uint32_t per_sm = t.chunk ? (t.chunk < kResumeCtasPerSm ? t.chunk : kResumeCtasPerSm) : kResumeCtasPerSm;
+        uint32_t grid = (uint32_t)g.sms * per_sm;
+        if (grid > A0.lanes) grid = A0.lanes;
+        cudaError_t e = cudaMemsetAsync(A0.cursor, 0, sizeof(uint32_t), g.stream);
+        if (e != cudaSuccess) return e;
+        return coop_launch((int)prec, R, g.coop_head, g.d_coop_scratch, grid, t.block, g.stream);
+    }
     const bool handoff = g.straggler_budget && g.d_coop_image && prec == 0;
     if (!handoff) return launch_lanes(prec, t, A0);
     DevArgs A = A0;
@@ -476,10 +494,23 @@ SGB_API int32_t gpu_kin_set_mech(const KinMech *mech, const KinMethod *method, c
     return 0;
 }
 
+// The tuning an advance of precision p runs: mode 1 (the reference's warp per cell) is the
+// cooperative decomposition with one warp per cell for FP64 and mixed; f32 lanes keep one thread
+// per cell in either mode.
+GpuKinTuning tuning_for(uint32_t p) {
+    GpuKinTuning t = g.tuning[p];
+    if (g.mode == 1 && p != 1 && t.kind != 3) {
+        t.kind = 3;
+        t.block = 32;
+        t.chunk = 0;
+    }
+    return t;
+}
+
 SGB_API int32_t gpu_kin_advance(const GpuKinLaunch *launch, float *kernel_ms) {
     uint32_t p = launch ? launch->precision : 0;
     if (p > 2) return (int32_t)cudaErrorInvalidValue;
-    return (int32_t)advance_sync(launch, g.tuning[p], kernel_ms);
+    return (int32_t)advance_sync(launch, tuning_for(p), kernel_ms);
 }
 
 SGB_API int32_t gpu_host_register(void *host, uint64_t size) {
@@ -509,7 +540,7 @@ SGB_API int32_t gpu_kin_advance_async(const GpuKinLaunch *launch, void *host_blo
     DevArgs A;
     fill_args(launch, &A);
     cudaEventRecord(g.kin_start, g.stream);
-    e = launch_advance(launch->precision, g.tuning[launch->precision], A);
+    e = launch_advance(launch->precision, tuning_for(launch->precision), A);
     cudaEventRecord(g.kin_stop, g.stream);
     if (e != cudaSuccess) return (int32_t)e;
     e = cudaMemcpy2DAsync(host_block, pitch, device_block, pitch, width, mutable_rows, cudaMemcpyDeviceToHost, g.stream);
@@ -609,9 +640,9 @@ SGB_API int32_t gpu_kin_wait(float *kernel_ms, float *total_ms) {
     return (int32_t)cudaGetLastError();
 }
 
-// Mode 1 (one warp per cell) is accepted for the reference's callers; both
-// decompositions produce the same bits, and this module runs every mode on its
-// per-lane kernels (thread per cell, optionally persistent).
+// Mode 1 (one warp per cell, gpu_api.h:108-110): FP64 and mixed advances run the cooperative
+// kernel with 32 threads per cell (FP64: the same bits as one thread per cell). Needs a
+// mechanism whose cooperative image could be built (any KinMech).
 SGB_API int32_t gpu_kin_set_mode(uint32_t mode) {
     if (mode > 1) return (int32_t)cudaErrorInvalidValue;
     g.mode = mode;
@@ -635,7 +666,12 @@ SGB_API int32_t gpu_kin_advance_queue(const GpuKinLaunch *launch, float *kernel_
 }
 
 SGB_API int32_t gpu_kin_set_tuning(const GpuKinTuning *t) {
-    if (!t || t->kind > 2 || t->block == 0 || (t->block & 31) || t->variant > 3 || t->chunk > 64) return (int32_t)cudaErrorInvalidValue;
+    if (!t || t->kind > 3 || t->block == 0 || (t->block & 31) || t->variant > 3 || t->chunk > 64) return (int32_t)cudaErrorInvalidValue;
+    if (t->kind == 3) {   // cooperative: 32..256 threads per cell
+        if (t->block > 256) return (int32_t)cudaErrorInvalidValue;
+        for (int p = 0; p < 3; ++p) g.tuning[p] = *t;
+        return 0;
+    }
     const uint32_t max_block = t->variant == 3 ? 512u : t->variant == 2 ? 256u : 128u;   // the variant's __launch_bounds__
     if (t->block > max_block || (t->variant >= 2 && t->kind != 2)) return (int32_t)cudaErrorInvalidValue;
     for (int p = 0; p < 3; ++p) g.tuning[p] = *t;
@@ -654,7 +690,7 @@ SGB_API int32_t gpu_kin_get_tuning(uint32_t precision, GpuKinTuning *t) {
 SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuKinTuning *best) {
     cudaError_t e = check_launch(launch);
     if (e != cudaSuccess) return (int32_t)e;
-    if (kind > 2) return (int32_t)cudaErrorInvalidValue;
+    if (kind > 4 || ((kind == 3 || kind == 4) && (!g.d_coop_image || launch->precision == 1))) return (int32_t)cudaErrorInvalidValue;
     const uint64_t P = launch->padded, n = g.mech.species_count;
     const uint64_t bytes_y = n * P * sizeof(double), bytes_v = P * sizeof(double);
     double *save = nullptr;
@@ -672,44 +708,46 @@ SGB_API int32_t gpu_kin_autotune(const GpuKinLaunch *launch, uint32_t kind, GpuK
         }
     };
     copy_all(true);
-    // candidates: block size x register budget x resident CTAs per SM (queue kernel)
-    struct Cand { uint32_t block, variant, ctas; };
-    const Cand cands[] = {{32, 0, 0}, {64, 0, 0}, {128, 0, 0}, {64, 1, 0}, {128, 1, 0},
-                          {128, 0, 1}, {64, 0, 2}, {64, 0, 3}, {128, 1, 2}, {128, 1, 3}};
-    const Cand sync_cands[] = {{128, 0, 2}, {256, 2, 1}, {128, 0, 1}, {128, 1, 4}, {512, 3, 1}};
+    // candidates: block size x register budget x resident CTAs per SM (lane kernels); threads per
+    // cell x CTAs per SM (cooperative kernel: cells per warp 1, 1/2, 1/4, 1/8); kind 4 = all of
+    // kind 2's and kind 3's, so the cells-per-warp decomposition is chosen by measurement too
+    struct Cand { uint32_t kind, block, variant, ctas; };
+    const Cand cands[] = {{1, 32, 0, 0}, {1, 64, 0, 0}, {1, 128, 0, 0}, {1, 64, 1, 0}, {1, 128, 1, 0},
+                          {1, 128, 0, 1}, {1, 64, 0, 2}, {1, 64, 0, 3}, {1, 128, 1, 2}, {1, 128, 1, 3}};
+    const Cand sync_cands[] = {{2, 128, 0, 2}, {2, 256, 2, 1}, {2, 128, 0, 1}, {2, 128, 1, 4}, {2, 512, 3, 1}};
+    const Cand coop_cands[] = {{3, 32, 0, 8}, {3, 64, 0, 4}, {3, 128, 0, 2}, {3, 256, 0, 1}};
+    std::vector<Cand> list;
+    if (kind == 0 || kind == 1)
+        for (const Cand &c : cands)
+            if (kind == 1 || c.ctas == 0) list.push_back(Cand{kind, c.block, c.variant, c.ctas});
+    if (kind == 2 || kind == 4) list.insert(list.end(), std::begin(sync_cands), std::end(sync_cands));
+    if (kind == 3 || kind == 4) list.insert(list.end(), std::begin(coop_cands), std::end(coop_cands));
     GpuKinTuning winner = g.tuning[launch->precision];
     winner.ms = 1e30f;
-    const Cand *list = kind == 2 ? sync_cands : cands;
-    const size_t count = kind == 2 ? sizeof(sync_cands) / sizeof(Cand) : sizeof(cands) / sizeof(Cand);
     // candidates that would grow the context's stack reservation are skipped, unless none fits
     size_t have = 0, least = (size_t)-1;
     cudaDeviceGetLimit(&have, cudaLimitStackSize);
-    for (size_t ci = 0; ci < count; ++ci) {
-        GpuKinTuning t = {kind, list[ci].block, list[ci].ctas, list[ci].variant, 0.0f};
+    for (const Cand &c : list) {
+        GpuKinTuning t = {c.kind, c.block, c.ctas, c.variant, 0.0f};
         size_t need = 0;
         if (local_bytes(launch->precision, t, &need) == cudaSuccess && need < least) least = need;
     }
     const bool keep_reservation = least <= have;
-    for (size_t ci = 0; ci < count; ++ci) {
-        const Cand &c = list[ci];
+    for (const Cand &c : list) {
         if (e != cudaSuccess) break;
-        if (kind == 0 && c.ctas != 0) continue;
-        {
-            GpuKinTuning t = {kind, c.block, c.ctas, c.variant, 0.0f};
-            size_t need = 0;
-            if (keep_reservation && local_bytes(launch->precision, t, &need) == cudaSuccess && need > have) continue;
-            float ms = 0.0f, best_ms = 1e30f;
-            for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {   // the faster of two runs
-                e = advance_sync(launch, t, &ms);
-                copy_all(false);
-                if (ms < best_ms) best_ms = ms;
-            }
-            ms = best_ms;
-            if (e != cudaSuccess) break;
-            if (ms < winner.ms) {
-                winner = t;
-                winner.ms = ms;
-            }
+        GpuKinTuning t = {c.kind, c.block, c.ctas, c.variant, 0.0f};
+        size_t need = 0;
+        if (keep_reservation && local_bytes(launch->precision, t, &need) == cudaSuccess && need > have) continue;
+        float ms = 0.0f, best_ms = 1e30f;
+        for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {   // the faster of two runs
+            e = advance_sync(launch, t, &ms);
+            copy_all(false);
+            if (ms < best_ms) best_ms = ms;
+        }
+        if (e != cudaSuccess) break;
+        if (best_ms < winner.ms) {
+            winner = t;
+            winner.ms = best_ms;
         }
     }
     cudaStreamSynchronize(g.stream);

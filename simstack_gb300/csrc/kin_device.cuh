@@ -26,6 +26,7 @@
 
 #include "../../include/simstack_gpu.h"
 #include "ptx.cuh"
+#include "tmem.cuh"
 
 namespace sgb {
 
@@ -963,10 +964,29 @@ __device__ __forceinline__ Df df_times_coef_u(Df a, double c) {
 
 // kLuStride > 0: the FP32 LU lives in shared memory, interleaved across the CTA's lanes
 // (element e of lane t at [e * kLuStride + t]), which frees registers for the double-float vectors.
-template <class Ops, class M, int kLuStride = 0>
+// kTmemCols > 0: the stage vectors K live in tensor memory -- the CTA allocates kTmemCols columns,
+// warp w uses lane quarter w % 4 and columns 256 (w / 4) + [0, 256), stage st at column 64 st:
+// K hi then K lo, 2N <= 64 floats -- instead of local memory (they are indexed by the stage).
+// Build-time switches of the CTA-synchronous kernel's barriers inside a refined step: after -J
+// and the factorisation (phase), and after every stage (stage). They keep the CTA's warps on the
+// same stretch of code; no data is shared between lanes, so results do not depend on them.
+// Measured on 1,048,576 cells x 10 s (256 threads, stage vectors in TMEM): stage barriers only
+// 558 ms, both 568 ms, none 678 ms (the instruction fetch is shared by fewer warps).
+#ifndef SGB_IR_PHASE_BARRIERS
+#define SGB_IR_PHASE_BARRIERS 0
+#endif
+#ifndef SGB_IR_STAGE_BARRIERS
+#define SGB_IR_STAGE_BARRIERS 1
+#endif
+
+template <class Ops, class M, int kLuStride = 0, int kTmemCols = 0>
 struct LaneIr {
+    static constexpr bool kPhaseBarriers = SGB_IR_PHASE_BARRIERS != 0, kStageBarriers = SGB_IR_STAGE_BARRIERS != 0;
     static constexpr int N = Ops::N, R = Ops::R, NNZ = Ops::NNZ, S = M::kStages;
     static constexpr size_t kSmemBytes = kLuStride ? (size_t)NNZ * kLuStride * sizeof(float) : 0;
+    static constexpr bool kTmemK = kTmemCols > 0;
+    static constexpr uint32_t kTmemAlloc = (uint32_t)kTmemCols;
+    static_assert(!kTmemK || (2 * N <= 64 && S * 64 <= 256), "stage vectors must fit 64 TMEM columns each, 4 stages");
 
     Ops ops;
     float yhi[N], ylo[N];
@@ -979,11 +999,59 @@ struct LaneIr {
     float lu_r[kLuStride ? 1 : NNZ];
     float *lu_s;
     float Yhi[N], Ylo[N], fhi[N], flo[N], bhi[N], blo[N];
-    float Khi[S][N], Klo[S][N];
+    float Khi[kTmemK ? 1 : S][N], Klo[kTmemK ? 1 : S][N];
     float x[N], x2[N];
+    uint32_t tmem_k;   // this thread's TMEM address of stage slot 0
 
     __device__ __forceinline__ void bind(unsigned char *smem) {
         if constexpr (kLuStride > 0) lu_s = (float *)smem + threadIdx.x;
+    }
+    __device__ __forceinline__ void bind_tmem(uint32_t base) { tmem_k = tmem_lane_addr(base, 256u * ((threadIdx.x >> 5) >> 2)); }
+
+    // stage vector st <-> kh, kl (TMEM slot or the local arrays)
+    __device__ __forceinline__ void k_store(int st, const float *kh, const float *kl) {
+        if constexpr (kTmemK) {
+            float v[2 * N];
+#pragma unroll
+            for (int s = 0; s < N; ++s) {
+                v[s] = kh[s];
+                v[N + s] = kl[s];
+            }
+            const uint32_t a = tmem_k + 64u * (uint32_t)st;
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c + 32 <= 2 * N; c += 32) tmem_st32(a + c, v + c);
+#pragma unroll
+            for (int c = (2 * N / 32) * 32; c < 2 * N; c += 2) tmem_st2(a + c, v[c], v[c + 1]);
+        } else {
+#pragma unroll
+            for (int s = 0; s < N; ++s) {
+                Khi[st][s] = kh[s];
+                Klo[st][s] = kl[s];
+            }
+        }
+    }
+    __device__ __forceinline__ void k_load(int st, float *kh, float *kl) {
+        if constexpr (kTmemK) {
+            float v[2 * N];
+            const uint32_t a = tmem_k + 64u * (uint32_t)st;
+            __syncwarp();
+#pragma unroll
+            for (int c = 0; c + 32 <= 2 * N; c += 32) tmem_ld32(a + c, v + c);
+#pragma unroll
+            for (int c = (2 * N / 32) * 32; c < 2 * N; c += 2) tmem_ld2(a + c, v[c], v[c + 1]);
+#pragma unroll
+            for (int s = 0; s < N; ++s) {
+                kh[s] = v[s];
+                kl[s] = v[N + s];
+            }
+        } else {
+#pragma unroll
+            for (int s = 0; s < N; ++s) {
+                kh[s] = Khi[st][s];
+                kl[s] = Klo[st][s];
+            }
+        }
     }
     __device__ __forceinline__ void lu_solve(float *v) {
         if constexpr (kLuStride > 0) ops.template solve<kLuStride>(lu_s, v);
@@ -1103,14 +1171,14 @@ struct LaneIr {
         // FP32 -J at the FP32 rounding of y, factorised
         if constexpr (kLuStride > 0) {
             ops.template neg_jac<kLuStride>(khi, yhi, lu_s);
-            if constexpr (kSync) __syncthreads();
+            if constexpr (kSync && kPhaseBarriers) __syncthreads();
             ops.template factor<kLuStride>((float)ghinv, lu_s);
         } else {
             ops.neg_jac(khi, yhi, lu_r);
-            if constexpr (kSync) __syncthreads();
+            if constexpr (kSync && kPhaseBarriers) __syncthreads();
             ops.factor((float)ghinv, lu_r);
         }
-        if constexpr (kSync) __syncthreads();
+        if constexpr (kSync && kPhaseBarriers) __syncthreads();
 
         bool f_at_y = false;   // f (fhi, flo) holds f(y)
 #pragma unroll 1
@@ -1131,9 +1199,11 @@ struct LaneIr {
                     const double a = M::a(A, packed + j);
                     if (a == 0.0) continue;
                     moved = true;
+                    float kh[N], kl[N];
+                    k_load(j, kh, kl);
                     for (int s = 0; s < N; ++s) {
                         if (s >= (int)nn) break;
-                        const Df v = df_acc(Df{Yhi[s], Ylo[s]}, df_times_coef_u(Df{Khi[j][s], Klo[j][s]}, a));
+                        const Df v = df_acc(Df{Yhi[s], Ylo[s]}, df_times_coef_u(Df{kh[s], kl[s]}, a));
                         Yhi[s] = v.hi;
                         Ylo[s] = v.lo;
                     }
@@ -1163,9 +1233,11 @@ struct LaneIr {
                 const double c = M::c(A, packed + j);
                 if (c == 0.0) continue;
                 const Df ch = df_from(c * hinv);
+                float kh[N], kl[N];
+                k_load(j, kh, kl);
                 for (int s = 0; s < N; ++s) {
                     if (s >= (int)nn) break;
-                    const Df v = df_acc(Df{bhi[s], blo[s]}, df_mul_u(ch, Df{Khi[j][s], Klo[j][s]}));
+                    const Df v = df_acc(Df{bhi[s], blo[s]}, df_mul_u(ch, Df{kh[s], kl[s]}));
                     bhi[s] = v.hi;
                     blo[s] = v.lo;
                 }
@@ -1181,35 +1253,55 @@ struct LaneIr {
             // one refinement sweep: r = b - ghinv x + J x (double-float), x2 = W32^-1 r
             ops.residual_df(khi, klo, yhi, ylo, x, bhi, blo, gd, x2);
             lu_solve(x2);
-            for (int s = 0; s < N; ++s) {
-                if (s >= (int)nn) break;
-                const Df v = df_two_sum(x[s], x2[s]);
-                Khi[st][s] = v.hi;
-                Klo[st][s] = v.lo;
+            {
+                float kh[N], kl[N];
+                for (int s = 0; s < N; ++s) {
+                    const Df v = df_two_sum(x[s], x2[s]);
+                    kh[s] = v.hi;
+                    kl[s] = v.lo;
+                }
+                k_store(st, kh, kl);
             }
-            if constexpr (kSync) __syncthreads();
+            if constexpr (kSync && kStageBarriers) __syncthreads();
         }
 
-        // y_new and the weighted RMS error, both in double-float
+        // y_new (accumulated in Y) and the error estimate (in b), stage vector by stage vector:
+        // per species the same operations in the same order as a species-by-species loop
+        for (int s = 0; s < N; ++s) {
+            if (s >= (int)nn) break;
+            Yhi[s] = yhi[s];
+            Ylo[s] = ylo[s];
+        }
+        bool first_e = true;
+#pragma unroll
+        for (int st = 0; st < S; ++st) {
+            if (st >= M::stages(A)) break;
+            const double mc = M::m(A, st), ec = M::e(A, st);
+            if (mc == 0.0 && ec == 0.0) continue;
+            float kh[N], kl[N];
+            k_load(st, kh, kl);
+            for (int s = 0; s < N; ++s) {
+                if (s >= (int)nn) break;
+                const Df kv{kh[s], kl[s]};
+                if (mc != 0.0) {
+                    const Df v = df_acc(Df{Yhi[s], Ylo[s]}, df_times_coef_u(kv, mc));
+                    Yhi[s] = v.hi;
+                    Ylo[s] = v.lo;
+                }
+                if (ec != 0.0) {
+                    const Df v = first_e ? df_times_coef_u(kv, ec) : df_acc(Df{bhi[s], blo[s]}, df_times_coef_u(kv, ec));
+                    bhi[s] = v.hi;
+                    blo[s] = v.lo;
+                }
+            }
+            if (ec != 0.0) first_e = false;
+        }
         const Df rtol = df_from(A.ctl.rtol), atol = df_from(A.ctl.atol);
         Df err2{0.0f, 0.0f};
         for (int s = 0; s < N; ++s) {
             if (s >= (int)nn) break;
-            Df yn{yhi[s], ylo[s]}, ye{0.0f, 0.0f};
-            bool first_e = true;
-#pragma unroll
-            for (int st = 0; st < S; ++st) {
-                if (st >= M::stages(A)) break;
-                const double mc = M::m(A, st), ec = M::e(A, st);
-                const Df kv{Khi[st][s], Klo[st][s]};
-                if (mc != 0.0) yn = df_acc(yn, df_times_coef_u(kv, mc));
-                if (ec != 0.0) {
-                    ye = first_e ? df_times_coef_u(kv, ec) : df_acc(ye, df_times_coef_u(kv, ec));
-                    first_e = false;
-                }
-            }
-            yn = df_norm(yn);
-            ye = df_norm(ye);
+            const Df yn = df_norm(Df{Yhi[s], Ylo[s]});
+            const Df ye = first_e ? Df{0.0f, 0.0f} : df_norm(Df{bhi[s], blo[s]});
             const Df ay = df_abs(Df{yhi[s], ylo[s]}), an = df_abs(yn);
             const Df scale = df_add(df_mul(rtol, df_less(ay, an) ? an : ay), atol);
             const float inv = 1.0f / scale.hi;

@@ -45,10 +45,47 @@ template <class Ops, class M, int V> struct LaneOf<Ops, M, 3, V> {
 #ifndef SGB_IR_SHARED_LU
 #define SGB_IR_SHARED_LU 1
 #endif
+// Build-time switch (default on): the refined lanes keep their stage vectors in tensor memory,
+// 256 columns per 128 threads of the launch bound (measured 568 against 580 ms on 1,048,576
+// cells x 10 s: the stage vectors leave local memory). Only with the shared-memory LU, whose
+// footprint (NNZ x launch bound x 4 bytes: 109 KB at 128 threads, 218 KB at 256 for the shipped
+// mechanism) caps how many CTAs an SM holds (228 KB of shared memory) so that together they
+// never ask for more than the SM's 512 columns: an allocation never waits.
+#ifndef SGB_IR_TMEM
+#define SGB_IR_TMEM 1
+#endif
+constexpr uint32_t kSmemPerSm = 233472;   // 228 KB
 template <class Ops, class M, int V> struct LaneOf<Ops, M, 4, V> {
     static constexpr int kStride = (SGB_IR_SHARED_LU && Ops::kStridedLu && Budget<V>::kThreads <= 256) ? Budget<V>::kThreads : 0;
-    typedef LaneIr<Ops, M, kStride> type;
+    static constexpr uint32_t kCols = 256u * (uint32_t)(Budget<V>::kThreads / 128);
+    static constexpr uint32_t kLuBytes = (uint32_t)Ops::NNZ * (uint32_t)(kStride > 0 ? kStride : 1) * 4u;
+    static constexpr bool kFits = kStride > 0 && (kSmemPerSm / kLuBytes) * kCols <= 512u;
+    static constexpr int kTmem = (SGB_IR_TMEM && kFits) ? (int)kCols : 0;
+    typedef LaneIr<Ops, M, kStride, kTmem> type;
 };
+
+// Tensor-memory columns of the lanes that keep data there: one warp allocates them for the CTA
+// before the lanes start and frees them after every lane is done (all threads pass both calls).
+template <class L> struct TmemCols { static constexpr uint32_t value = 0; };
+template <class Ops, class M, int S, int C> struct TmemCols<LaneIr<Ops, M, S, C>> { static constexpr uint32_t value = (uint32_t)C; };
+
+template <class L> __device__ __forceinline__ void lanes_tmem_open(L &lane, uint32_t *slot) {
+    if constexpr (TmemCols<L>::value > 0) {
+        if (threadIdx.x < 32) tmem_alloc(slot, TmemCols<L>::value);
+        tmem_fence_before_sync();
+        __syncthreads();
+        tmem_fence_after_sync();
+        lane.bind_tmem(*slot);
+    }
+}
+template <class L> __device__ __forceinline__ void lanes_tmem_close(const uint32_t *slot) {
+    if constexpr (TmemCols<L>::value > 0) {
+        tmem_fence_before_sync();
+        __syncthreads();
+        tmem_fence_after_sync();
+        if (threadIdx.x < 32) tmem_dealloc(*slot, TmemCols<L>::value);
+    }
+}
 
 // Both kernels keep every lane of a warp in the loop until the whole warp is
 // out of work, and vote (__any_sync) once per iteration: the vote is a
@@ -65,9 +102,12 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
         return;
     }
     L.bind(smem);
+    __shared__ uint32_t tmem_slot;
+    lanes_tmem_open(L, &tmem_slot);
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     bool have = i < A.lanes;
     if (have) L.load(A, i);
+    else if (TmemCols<decltype(L)>::value > 0) L.load(A, 0);   // a finite state for lanes that attempt with no cell
     for (;;) {
         bool need = false;
         if (have) {
@@ -78,8 +118,10 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
             }
         }
         if (!__any_sync(0xffffffffu, need)) break;
-        if (need) L.attempt(A);
+        if constexpr (TmemCols<decltype(L)>::value > 0) L.attempt(A, need);   // warp-collective TMEM access: every lane
+        else if (need) L.attempt(A);
     }
+    lanes_tmem_close<decltype(L)>(&tmem_slot);
 }
 
 template <class Ops, class M, int PREC, int V>
@@ -91,6 +133,9 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
         return;
     }
     L.bind(smem);
+    __shared__ uint32_t tmem_slot;
+    lanes_tmem_open(L, &tmem_slot);
+    if (TmemCols<decltype(L)>::value > 0) L.load(A, 0);   // a finite state for lanes that attempt with no cell
     bool have = false, exhausted = false;
     uint32_t cell = 0;
     for (;;) {
@@ -113,8 +158,10 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
             have = false;
         }
         if (!__any_sync(0xffffffffu, need)) break;
-        if (need) L.attempt(A);
+        if constexpr (TmemCols<decltype(L)>::value > 0) L.attempt(A, need);   // warp-collective TMEM access: every lane
+        else if (need) L.attempt(A);
     }
+    lanes_tmem_close<decltype(L)>(&tmem_slot);
 }
 
 // CTA-synchronous persistent queue: like kin_queue_kernel, but the whole CTA
@@ -134,6 +181,8 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
     }
     L.bind(smem);
     if (A.lanes == 0) return;
+    __shared__ uint32_t tmem_slot;
+    lanes_tmem_open(L, &tmem_slot);
     L.load(A, 0);   // a finite state for lanes that never get a cell
     bool have = false, exhausted = false;
     uint32_t cell = 0;
@@ -159,6 +208,7 @@ __global__ void __launch_bounds__(Budget<V>::kThreads, Budget<V>::kMinBlocks) ki
         if (!__syncthreads_or(need)) break;
         L.template attempt<true>(A, need);
     }
+    lanes_tmem_close<decltype(L)>(&tmem_slot);
 }
 
 // Launch shape chosen by the host (module tuning or the autotuner).

@@ -104,6 +104,26 @@ def test_coop_f64_large_mechanism(module, oracle_lib):
     module.reset_arena()
 
 
+def test_coop_large_mechanism_64_cells(module, oracle_lib):
+    """200 species / 1,200 reactions, 64 cells x 0.5 s (~475 steps per cell): the FP64 cooperative
+    path bit for bit against the oracle, and the mixed cooperative path (FP32 LU in shared memory,
+    FP64 refinement residual) within 1e-5 of it on every species of every cell (|a-b| / max(|b|,
+    atol), no filter)."""
+    pm, om = synthetic_pair(oracle_lib, 4, 200, 1200)
+    ctl = dict(rtol=1e-4, atol=1e-12, max_steps=200000)
+    module.coop_set_mech(pm, sg.method("rodas3"), sg.control(**ctl))
+    z0 = sg.synthetic_cells(pm, 64, seed=5)
+    z, zm, ref = z0.copy(), z0.copy(), z0.copy()
+    module.coop_integrate(z, 0.5, precision=0, lane_count=64)
+    module.coop_integrate(zm, 0.5, precision=2, lane_count=64)
+    om.advance("rodas3", oracle_lib.control(**ctl), ref.as_dict(), ref.padded, 0, 64, 0.5, 0, 0)
+    assert_state(z, ref, 64)
+    a, b = zm["y"][:, :64], ref["y"][:, :64]
+    rel = np.abs(a - b) / np.maximum(np.abs(b), 1e-12)
+    assert zm["failed"][:64].max() == 0.0 and rel.max() <= 1e-5, rel.max()
+    module.reset_arena()
+
+
 def test_coop_mixed_accuracy(module, oracle_lib):
     """Mixed cooperative path (FP32 LU in shared memory + FP64 refinement) vs FP64, 60-species mechanism."""
     pm = sg.Model.synthetic(seed=7, species=60, reactions=300, bimolecular=0.7, products=1)
