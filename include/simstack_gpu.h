@@ -453,6 +453,38 @@ SGB_API int32_t gpu_serve_stats(GpuServeStats *stats);
 SGB_API int32_t gpu_serve_close(void);
 
 /* ---------------------------------------------------------------------------
+ * NFT film transport of one coupling window (replaces src/sim/nft.cpp:1028-1106,
+ * nft_transport<V>, called per group from nft_group_window, nft.cpp:1142-1152).
+ * Device copies of the reference's group arrays in the reference's byte layout
+ * (nft.cpp:134-178), packed group after group (groups of 8 channels = lanes):
+ *   rows    [groups][cells]  NftRow      f32 f[9][8]                   288 B  in/out
+ *   hot     [groups][cells]  NftCellHot  f32 c, kT, bT, ko [8]         128 B  reads c, ko; writes kT, bT
+ *   cold    [groups][cells]  NftCellCold f64 vol_L[8], f32 inv_v, kw, kr, ge, ev, depth, phi, vel [8]
+ *                                                                    320 B  reads kw, kr, ge, ev
+ *   sites   [groups][sites]  NftSiteRow                               1,152 B reads drop, accumulates removed
+ *   out_sum [groups][9][8]   sum over substeps of the outlet deltas (NftGroup::out_sum)   out
+ *   evap_kg [groups][8]      film evaporation this window (NftGroup::lp.evap_kg)         out
+ * ref[9] = this window's inlet (NftSystem::ref); T_amb, radiant, e0, es_slope from
+ * NftEnv. flush_denormals = 1 reproduces the reference as it runs on x86-64 hosts
+ * (NftFlushDenormals: FTZ/DAZ around the group's work), 0 as it runs elsewhere (IEEE);
+ * either way the result is bit-identical to nft_transport<f32x8> / <f32> there.
+ * rows, hot, cold and sites 16-byte aligned; cells >= 1. Synchronous on the module
+ * stream; kernel_ms = device time. */
+typedef struct GpuNftTransport {
+    float *rows;
+    float *hot;
+    const float *cold;
+    float *sites;
+    float *out_sum;
+    float *evap_kg;
+    uint32_t groups, cells, sites_count, site_offset, site_stride, substeps;
+    uint32_t flush_denormals;
+    float ref[9];
+    float T_amb, radiant, e0, es_slope;
+} GpuNftTransport;
+SGB_API int32_t gpu_nft_transport(const GpuNftTransport *t, float *kernel_ms);
+
+/* ---------------------------------------------------------------------------
  * Host-side mechanism compiler: src/sim/kinetics/kin_build.cpp:78-244 and
  * air_mech.cpp:30-108, 205-276. Builds the reference-layout KinMech (same
  * pattern, pivot order and bytes as kin_mech_finalize), rate constants and

@@ -323,6 +323,10 @@ def ref() -> C.CDLL:
         L.ref_dbd_run.restype = i32
         L.ref_air_advance_threads.argtypes = [i32, C.POINTER(Control), C.POINTER(LaneArrays), u32, u32, d, u32]
         L.ref_air_advance_threads.restype = i32
+        L.ref_gpu_load.argtypes = [C.c_char_p, u64]
+        L.ref_gpu_load.restype = i32
+        L.ref_dbd_hybrid_run.argtypes = [vp, u32, u32, i32, u32, d, i32, d, C.POINTER(Control), u32, u32, i32, vp, vp, vp]
+        L.ref_dbd_hybrid_run.restype = i32
         _ref = L
     return _ref
 
@@ -379,6 +383,32 @@ def ref_dbd_run(block: np.ndarray, count: int, padded: int, pulsed: bool, steps:
                            C.byref(ctl), threads, int(f32_lanes))
     if rc != 0:
         raise RuntimeError(f"ref_dbd_run: {rc}")
+
+
+def ref_gpu_load(path: str, arena_bytes: int) -> None:
+    """Loads a GPU module with the reference's own loader (platform/linux_gpu.cpp:7-31),
+    which calls its gpu_init: do this in a process that has not initialised the module."""
+    rc = ref().ref_gpu_load(path.encode(), arena_bytes)
+    if rc != 0:
+        raise RuntimeError(f"ref_gpu_load({path}): {rc}")
+
+
+def ref_dbd_hybrid_run(block: np.ndarray, count: int, padded: int, pulsed: bool, steps: int, dt: float, ctl: Control,
+                       threads: int, precision: int, force_split: int = -1, chained: bool = False,
+                       residence_s: float = 0.0):
+    """`steps` master steps of the reference's zone driver with its hybrid CPU+GPU advance
+    (dbd.cpp:336-463) on the module loaded by ref_gpu_load, in place. Returns per-step arrays
+    (split, step wall ms, GPU launch-to-completion ms)."""
+    assert block.dtype == np.float64 and block.flags["C_CONTIGUOUS"]
+    split = np.zeros(steps, np.uint32)
+    step_ms = np.zeros(steps, np.float32)
+    gpu_ms = np.zeros(steps, np.float32)
+    rc = ref().ref_dbd_hybrid_run(block.ctypes.data, count, padded, 0 if pulsed else 1, steps, dt, int(chained),
+                                  residence_s, C.byref(ctl), threads, precision, force_split, split.ctypes.data,
+                                  step_ms.ctypes.data, gpu_ms.ctypes.data)
+    if rc != 0:
+        raise RuntimeError(f"ref_dbd_hybrid_run: {rc}")
+    return split, step_ms, gpu_ms
 
 
 def ref_robertson(method: str, ctl: Control, t_end: float = 40.0):
@@ -454,3 +484,124 @@ class RefBigMechanism:
         rc = self.L.ref_big_advance(self.h, METHOD_IDS[method], C.byref(ctl), C.byref(la), begin, end, duration, variant)
         if rc != 0:
             raise RuntimeError(f"ref_big_advance: {rc}")
+
+
+# ---------------------------------------------------------------------------
+# The reference's NFT channel system (oracle/_ref/libref_nft.so, only where the
+# reference sources exist): nft_run, the window split at the transport, and
+# nft_transport on caller arrays.
+
+REF_NFT_LIB = os.path.join(HERE, "_ref", "libref_nft.so")
+NFT_LANES, NFT_FIELDS = 8, 9
+_ref_nft = None
+
+
+def ref_nft_available() -> bool:
+    return os.path.exists(REF_NFT_LIB)
+
+
+def ref_nft() -> C.CDLL:
+    global _ref_nft
+    if _ref_nft is None:
+        L = C.CDLL(REF_NFT_LIB)
+        vp, u32, f32, u64 = C.c_void_p, C.c_uint32, C.c_float, C.c_uint64
+        L.ref_nft_create.argtypes = [u32, f32, u32]
+        L.ref_nft_create.restype = vp
+        L.ref_nft_destroy.argtypes = [vp]
+        L.ref_nft_info.argtypes = [vp, vp]
+        L.ref_nft_run.argtypes = [vp, u32, u32]
+        for name in ("ref_nft_window_prepare", "ref_nft_window_transport", "ref_nft_window_finish"):
+            getattr(L, name).argtypes = [vp]
+        L.ref_nft_window_inputs.argtypes = [vp, vp, vp]
+        L.ref_nft_window_inputs.restype = u32
+        L.ref_nft_group_arrays.argtypes = [vp, u32, vp]
+        L.ref_nft_digest.argtypes = [vp]
+        L.ref_nft_digest.restype = u64
+        L.ref_nft_layout.argtypes = [vp]
+        L.ref_nft_transport_arrays.argtypes = [vp, vp, vp, vp, vp, vp, u32, u32, u32, u32, vp, vp, u32, u32]
+        _ref_nft = L
+    return _ref_nft
+
+
+def ref_nft_layout() -> dict:
+    out = np.zeros(16, np.uint64)
+    ref_nft().ref_nft_layout(out.ctypes.data)
+    keys = ("lanes", "fields", "row_bytes", "hot_bytes", "cold_bytes", "site_bytes", "hot_c", "hot_kT", "hot_bT",
+            "hot_ko", "cold_kw", "cold_kr", "cold_ge", "cold_ev", "site_drop", "site_removed")
+    return {k: int(v) for k, v in zip(keys, out)}
+
+
+class RefNftSystem:
+    """A reference NftSystem (nft_init with nft_default_params, rails / length / plants set)."""
+
+    def __init__(self, rails: int, rail_length_m: float = 0.0, plants_per_rail: int = 0):
+        self.L = ref_nft()
+        self.h = self.L.ref_nft_create(rails, rail_length_m, plants_per_rail)
+        info = np.zeros(8, np.uint32)
+        self.L.ref_nft_info(self.h, info.ctypes.data)
+        (self.rails, self.groups, self.cells, self.sites, self.site_offset, self.site_stride, self.substeps,
+         self.lanes) = (int(v) for v in info)
+        self.layout = ref_nft_layout()
+
+    def close(self):
+        if self.h:
+            self.L.ref_nft_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def run(self, windows: int, scalar_lanes: bool = False):
+        self.L.ref_nft_run(self.h, windows, int(scalar_lanes))
+
+    def prepare(self):
+        self.L.ref_nft_window_prepare(self.h)
+
+    def transport(self):
+        self.L.ref_nft_window_transport(self.h)
+
+    def finish(self):
+        self.L.ref_nft_window_finish(self.h)
+
+    def inputs(self):
+        """This window's inlet ref[9], env (T_amb, radiant, e0, es_slope) and substeps."""
+        ref = np.zeros(NFT_FIELDS, np.float32)
+        env = np.zeros(4, np.float32)
+        self.substeps = int(self.L.ref_nft_window_inputs(self.h, ref.ctypes.data, env.ctypes.data))
+        return ref, env, self.substeps
+
+    def digest(self) -> int:
+        return int(self.L.ref_nft_digest(self.h))
+
+    def group_views(self, g: int) -> dict:
+        """numpy views (float32, no copy) of group g's arrays in the reference's layout."""
+        ptrs = (C.c_void_p * 6)()
+        self.L.ref_nft_group_arrays(self.h, g, ptrs)
+        lay = self.layout
+
+        def view(p, nbytes):
+            return np.ctypeslib.as_array((C.c_float * (nbytes // 4)).from_address(p))
+
+        return {"rows": view(ptrs[0], lay["row_bytes"] * self.cells),
+                "hot": view(ptrs[1], lay["hot_bytes"] * self.cells),
+                "cold": view(ptrs[2], lay["cold_bytes"] * self.cells),
+                "sites": view(ptrs[3], lay["site_bytes"] * self.sites),
+                "out_sum": view(ptrs[4], 4 * NFT_FIELDS * NFT_LANES),
+                "evap_kg": view(ptrs[5], 4 * NFT_LANES)}
+
+
+def ref_nft_transport_arrays(rows, hot, cold, sites, cells, sites_count, site_offset, site_stride, ref, env, substeps,
+                             ieee: bool = False):
+    """The reference's nft_transport<f32x8> of one group over float32 arrays (32-byte aligned),
+    in place, in this host's denormal mode (ieee = False) or without it; returns
+    (out_sum[9*8], evap_kg[8])."""
+    for a in (rows, hot, cold, sites):
+        assert a.dtype == np.float32 and a.ctypes.data % 32 == 0 and a.flags["C_CONTIGUOUS"]
+    out_sum = np.zeros(NFT_FIELDS * NFT_LANES, np.float32)
+    evap = np.zeros(NFT_LANES, np.float32)
+    ref = np.ascontiguousarray(ref, np.float32)
+    env = np.ascontiguousarray(env, np.float32)
+    ref_nft().ref_nft_transport_arrays(rows.ctypes.data, hot.ctypes.data, cold.ctypes.data, sites.ctypes.data,
+                                       out_sum.ctypes.data, evap.ctypes.data, cells, sites_count, site_offset,
+                                       site_stride, ref.ctypes.data, env.ctypes.data, substeps, int(ieee))
+    return out_sum, evap

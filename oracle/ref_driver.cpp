@@ -10,7 +10,8 @@
 // air_mech.cpp), kin_eval_rate_constants, kin_integrate (kin_solver.h),
 // dbd_advance_cpu / dbd_advance_group (dbd.cpp, dbd_lanes.h) with the
 // generated AirGenOps or the table walk, f64 / f64x4 / f32 / f32x8 lanes,
-// and air_source_delta.
+// and air_source_delta; and, with a GPU module loaded by the reference's own
+// loader (linux_load_gpu_module), the hybrid CPU+GPU driver dbd_advance_hybrid.
 
 // Profiler shim: the reference's base_debug.h reads the x86 TSC; the solver
 // only uses its TIMED_FUNCTION() markers, which compile to nothing here.
@@ -22,6 +23,8 @@ struct DebugTable;
 #include <stdio.h>
 #include <stdlib.h>
 #include <math.h>
+#include <dlfcn.h>
+#include <time.h>
 
 #include <atomic>
 #include <thread>
@@ -29,6 +32,7 @@ struct DebugTable;
 
 #include "sim_platform.h"
 #include "sim/dbd.cpp"
+#include "platform/linux_gpu.cpp"
 
 #define REF_API extern "C" __attribute__((visibility("default")))
 
@@ -182,13 +186,8 @@ REF_API s32 ref_air_advance_threads(s32 method_id, const RefControl *rc, const R
 // (dbd_scene.cpp:232-265) without the scene around it. mode 0 pulsed, 1 averaged; the advance
 // on `threads` host threads (dbd_advance_threads) when threads > 1, f32x8 Delta lanes when
 // f32_lanes (the sweep scene's default precision), else f64x4 lanes.
-REF_API s32 ref_dbd_run(f64 *block, u32 count, u32 padded, s32 mode, u32 steps, f64 dt, s32 chained, f64 residence_s,
-                        const RefControl *rc, u32 threads, u32 f32_lanes) {
-    KinModel *model = air_model();
-    if (padded % 8) return -1;
-    KinMethod method = kin_method(KinMethod_Rodas3);
-    KinControl ctl = to_control(rc);
-    AirSourceModel source = air_source_defaults();
+// The zone block's rows in the reference's order (dbd.cpp:60-83), over a caller's f64 block.
+static DbdZones zones_over(f64 *block, u32 count, u32 padded, const KinModel *model) {
     DbdZones z = {};
     z.count = count;
     z.padded = padded;
@@ -205,6 +204,18 @@ REF_API s32 ref_dbd_run(f64 *block, u32 count, u32 padded, s32 mode, u32 steps, 
     }
     z.block = block;
     z.block_count = off;
+    z.mutable_count = (ns + 5) * p;   // y, h, steps, rejects, pulses, failed: the solver-written prefix
+    return z;
+}
+
+REF_API s32 ref_dbd_run(f64 *block, u32 count, u32 padded, s32 mode, u32 steps, f64 dt, s32 chained, f64 residence_s,
+                        const RefControl *rc, u32 threads, u32 f32_lanes) {
+    KinModel *model = air_model();
+    if (padded % 8) return -1;
+    KinMethod method = kin_method(KinMethod_Rodas3);
+    KinControl ctl = to_control(rc);
+    AirSourceModel source = air_source_defaults();
+    DbdZones z = zones_over(block, count, padded, model);
     f64 t = 0.0;   // the scene clock: t1 = t + dt, then t = t1 (dbd_scene.cpp:232, 266)
     for (u32 s = 0; s < steps; ++s) {
         f64 t0 = t, t1 = t + dt;
@@ -229,6 +240,80 @@ REF_API s32 ref_dbd_run(f64 *block, u32 count, u32 padded, s32 mode, u32 steps, 
         t = t1;
     }
     return 0;
+}
+
+// The reference's GPU module table, filled by its own loader from the module at `path`
+// (platform/linux_gpu.cpp:7-31: dlopen, the 16 exports by name, gpu_init(0, arena)).
+// Loaded once per process; a second path is refused.
+static GpuAPI g_gpu;
+static char g_gpu_path[1024];
+
+REF_API s32 ref_gpu_load(const char *path, u64 arena_bytes) {
+    if (g_gpu.available) return strcmp(path, g_gpu_path) == 0 ? 0 : -2;
+    if (!linux_load_gpu_module(path, arena_bytes, &g_gpu)) return -1;
+    snprintf(g_gpu_path, sizeof(g_gpu_path), "%s", path);
+    return 0;
+}
+
+static u64 ref_now_ns(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (u64)ts.tv_sec * 1000000000ull + (u64)ts.tv_nsec;
+}
+
+// `steps` master steps of dt of dbd_scene_step's sequence (dbd_scene.cpp:232-265) with the
+// reference's hybrid advance, dbd_advance_hybrid (dbd.cpp:336-463): lanes [0, split) on the
+// loaded GPU module (gpu_kin_set_mech, gpu_host_register, gpu_kin_advance_async,
+// gpu_kin_wait), lanes [split, padded) on `threads` host threads through
+// dbd_advance_threads, the split chosen by its own measured search (force_split < 0) or
+// fixed (force_split >= 0). Per step: the split used, the step's wall time (ms), and the
+// module's launch-to-completion time (ms, 0 for a CPU-only step). The block is page-locked
+// for the run and released at the end. precision: 0 FP64 lanes, 1 f32 Delta lanes.
+REF_API s32 ref_dbd_hybrid_run(f64 *block, u32 count, u32 padded, s32 mode, u32 steps, f64 dt, s32 chained,
+                               f64 residence_s, const RefControl *rc, u32 threads, u32 precision, s32 force_split,
+                               u32 *split_out, f32 *step_ms_out, f32 *gpu_ms_out) {
+    if (!g_gpu.available) return -1;
+    KinModel *model = air_model();
+    if (padded % 8 || threads == 0) return -1;
+    KinMethod method = kin_method(KinMethod_Rodas3);
+    KinControl ctl = to_control(rc);
+    AirSourceModel source = air_source_defaults();
+    DbdZones z = zones_over(block, count, padded, model);
+    s32 err = g_gpu.gpu_kin_set_mech(&model->mech, &method, &ctl);
+    if (err) return err;
+    g_gpu.gpu_arena_reset();
+    PlatformAPI api = {};
+    api.add_work_entry = ref_add_work_entry;
+    api.complete_all_work = ref_complete_all_work;
+    api.now_ns = ref_now_ns;
+    PlatformWorkQueue queue;
+    queue.threads = threads;
+    static u8 frame_memory[1 << 20];
+    DbdGpu g = {};
+    DbdHybrid *hy = (DbdHybrid *)calloc(1, sizeof(DbdHybrid));
+    hy->force_split = force_split;
+    f64 t = 0.0;
+    for (u32 s = 0; s < steps && !err; ++s) {
+        f64 t0 = t, t1 = t + dt;
+        dbd_zones_prepare_source(&z, &g_air_sp, &source, (DbdDischargeMode)mode, t0, t1);
+        u32 split = force_split >= 0 ? (u32)force_split : hy->split;
+        split = Minimum(split & ~7u, padded);
+        Arena frame = arena_make(frame_memory, sizeof(frame_memory));
+        u64 a = ref_now_ns();
+        err = dbd_advance_hybrid(&z, &g_gpu, &g, hy, dt, precision, &model->mech, &method, &ctl, 1, &api, &queue,
+                                 threads, &frame);
+        u64 b = ref_now_ns();
+        if (split_out) split_out[s] = split;
+        if (step_ms_out) step_ms_out[s] = (f32)((f64)(b - a) * 1e-6);
+        if (gpu_ms_out) gpu_ms_out[s] = split ? hy->last_gpu_ms : 0.0f;
+        dbd_zones_commit_pulses(&z);
+        if (chained) dbd_flow_exchange(&z, &g_air_sp, residence_s, dt);
+        t = t1;
+    }
+    if (hy->registered) g_gpu.gpu_host_unregister(hy->registered_block);
+    free(hy);
+    g_gpu.gpu_arena_reset();
+    return err;
 }
 
 // Robertson (test_kinetics.cpp:151-180 set-up): one scalar integration.

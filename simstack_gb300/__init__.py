@@ -128,6 +128,13 @@ class GpuAirSource(C.Structure):
     _fields_ = [(n, C.c_double) for n in ("g_O2_diss", "f_O1D", "g_N2A", "g_N2_diss", "g_OH_per_100eV", "filament_J_cm3")]
 
 
+class GpuNftTransport(C.Structure):
+    _fields_ = [(n, C.c_void_p) for n in ("rows", "hot", "cold", "sites", "out_sum", "evap_kg")] + \
+               [(n, C.c_uint32) for n in ("groups", "cells", "sites_count", "site_offset", "site_stride", "substeps",
+                                          "flush_denormals")] + \
+               [("ref", C.c_float * 9)] + [(n, C.c_float) for n in ("T_amb", "radiant", "e0", "es_slope")]
+
+
 class GpuError(RuntimeError):
     def __init__(self, code: int, where: str):
         msg = lib().gpu_error_string(code).decode() if _lib is not None else str(code)
@@ -220,6 +227,7 @@ def lib() -> C.CDLL:
             "gpu_dbd_commit_pulses": (i32, [C.POINTER(GpuDbdZones)]),
             "gpu_dbd_flow_exchange": (i32, [C.POINTER(GpuDbdZones), d, d]),
             "gpu_dbd_step": (i32, [C.POINTER(GpuDbdZones), C.POINTER(GpuAirSource), u32, d, d, u32, u32, d, C.POINTER(f)]),
+            "gpu_nft_transport": (i32, [C.POINTER(GpuNftTransport), C.POINTER(f)]),
             "sgb_workload_air": (None, [u64, u64, u32, u32, d, d, d, d, vp, vp, vp, vp]),
             "sgb_workload_air_source": (None, [u64, u64, u32, u32, d, d, vp, vp, vp, vp]),
             "sgb_workload_synthetic_mech": (vp, [u64, u32, u32, d, u32, d, d, vp]),
@@ -805,3 +813,55 @@ class Server:
 
     def __exit__(self, *exc):
         self.close()
+
+
+# --------------------------------------------------------------------------
+# NFT film transport (gpu_nft_transport): the reference's group arrays on the device.
+
+NFT_LANES, NFT_FIELDS = 8, 9
+# floats per element of each group array (src/sim/nft.cpp:134-178)
+NFT_FLOATS = {"rows": 72, "hot": 32, "cold": 80, "sites": 288}
+
+
+class NftTransport:
+    """Device copies of G groups' NFT arrays (float32 views of the reference's layouts:
+    rows [G][cells][9][8], hot [G][cells][4][8], cold [G][cells] 80 floats, sites
+    [G][sites] 288 floats), packed group after group in the module's arena, and one
+    window's transport over all of them."""
+
+    def __init__(self, module: "Module", groups: int, cells: int, sites: int, site_offset: int, site_stride: int):
+        self.groups, self.cells, self.sites = groups, cells, sites
+        self.site_offset, self.site_stride = site_offset, site_stride
+        self.shape = {"rows": groups * cells * 72, "hot": groups * cells * 32, "cold": groups * cells * 80,
+                      "sites": max(1, groups * sites * 288), "out_sum": groups * 72, "evap_kg": groups * 8}
+        self.dev = {}
+        for name, n in self.shape.items():
+            self.dev[name] = module.alloc(4 * n)
+            if not self.dev[name]:
+                raise GpuError(2, f"NftTransport: arena full ({name})")
+
+    def upload(self, name: str, host: np.ndarray) -> None:
+        host = np.ascontiguousarray(host, np.float32)
+        assert host.size == self.shape[name] or (name == "sites" and self.sites == 0), (name, host.size)
+        if host.size:
+            check(lib().gpu_copy_to_device(self.dev[name], _p(host), host.nbytes), f"upload {name}")
+
+    def download(self, name: str) -> np.ndarray:
+        out = np.empty(self.shape[name], np.float32)
+        check(lib().gpu_copy_to_host(_p(out), self.dev[name], out.nbytes), f"download {name}")
+        return out
+
+    def run(self, ref, T_amb: float, radiant: float, e0: float, es_slope: float, substeps: int,
+            flush_denormals: bool = True) -> float:
+        t = GpuNftTransport()
+        for name in ("rows", "hot", "cold", "sites", "out_sum", "evap_kg"):
+            setattr(t, name, self.dev[name])
+        t.groups, t.cells, t.sites_count = self.groups, self.cells, self.sites
+        t.site_offset, t.site_stride, t.substeps = self.site_offset, self.site_stride, substeps
+        t.flush_denormals = int(flush_denormals)
+        for k in range(NFT_FIELDS):
+            t.ref[k] = float(np.float32(ref[k]))
+        t.T_amb, t.radiant, t.e0, t.es_slope = (float(np.float32(v)) for v in (T_amb, radiant, e0, es_slope))
+        ms = C.c_float()
+        check(lib().gpu_nft_transport(C.byref(t), C.byref(ms)), "gpu_nft_transport")
+        return ms.value

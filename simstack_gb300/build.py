@@ -88,6 +88,7 @@ def build(force: bool = False, jobs: int | None = None) -> str:
         ("static_scratch.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "static_scratch.cu")]),
         ("serve.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "serve.cu")]),
         ("dbd_driver.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "dbd_driver.cu")]),
+        ("nft_transport.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "nft_transport.cu")]),
         ("kern_coop.o", [NVCC, *NV_FLAGS, "-c", os.path.join(CSRC, "kern_coop.cu")]),
         ("coop_build.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "coop_build.cpp")]),
         ("mech.o", [CXX, *CXX_FLAGS, "-c", os.path.join(CSRC, "mech.cpp")]),
