@@ -536,6 +536,19 @@ template <class T> static inline T step_factor(T err, u32 order) {
     return vmin(vmax(fac, (T)0.2), (T)6.0);
 }
 
+// The mixed lanes' step-size factor (the GPU's step_factor_mixed): order 3 from the FP32
+// cube-root chain, one division-free FP64 Newton step for e^(-1/3), fac = 0.9 w.
+static inline double step_factor_mixed(double err, u32 order) {
+    if (order != 3) return step_factor(err, order);
+    const double e = vmin(vmax(err, 1e-4), 1e4);
+    const float g = cbrt_clamped((float)e);
+    double w = (double)(1.0f / g);
+    const double w3 = w * w * w;
+    w = w * (4.0 - e * w3) * (1.0 / 3.0);
+    const double fac = 0.9 * w;
+    return vmin(vmax(fac, 0.2), 6.0);
+}
+
 template <class T> static void eval_fun(const Mechanism &m, const T *k, const T *src, const T *y, T *f) {
     const u32 n = m.n();
     for (u32 s = 0; s < n; ++s) f[s] = src[s];
@@ -1368,7 +1381,7 @@ static void integrate_mixed_ir(const Mechanism &m, const Method &me, const Contr
         bool last = h_wanted >= remaining;
         double hs = last ? remaining : vmin(h_wanted, h_cap);
         const double ghinv = 1.0 / (hs * me.gamma0), hinv = 1.0 / hs;
-        const Df2 gd = df_from(ghinv);
+        const Df2 gd = df_from(ghinv), hd = df_from(hinv);
 
         eval_fun_dfl(m, w.kd.data(), w.sd.data(), y, fy.data());
         for (u32 s = 0; s < n; ++s) yhi[s] = y[s].hi;
@@ -1397,7 +1410,7 @@ static void integrate_mixed_ir(const Mechanism &m, const Method &me, const Contr
             for (u32 j = 0; j < stg; ++j) {
                 double c = me.c[packed + j];
                 if (c == 0.0) continue;
-                const Df2 ch = df_from(c * hinv);
+                const Df2 ch = df_mul(df_from(c), hd);   // c / h in double-float
                 for (u32 s = 0; s < n; ++s) b[s] = df_acc(b[s], df_mul_u(ch, K[j][s]));
             }
             for (u32 s = 0; s < n; ++s) b[s] = df_norm(b[s]);
@@ -1433,7 +1446,7 @@ static void integrate_mixed_ir(const Mechanism &m, const Method &me, const Contr
         }
         double err = std::sqrt(df_to(err2) * inv_n);
         if (!finite(err)) err = 1e10;
-        double fac = step_factor(err, me.order);
+        double fac = step_factor_mixed(err, me.order);
         bool ok = err <= 1.0 || hs <= ctl.h_min;
         if (ctl.fixed_step) { ok = true; fac = 1.0; }
         if (ok) {

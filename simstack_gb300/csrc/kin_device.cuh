@@ -75,6 +75,8 @@ __device__ __forceinline__ Df df_from(double d) {
     return Df{h, (float)(d - (double)h)};   // d - h is exact in FP64
 }
 __device__ __forceinline__ double df_to(Df a) { return (double)a.hi + (double)a.lo; }
+// df_from of a compile-time constant
+__host__ __device__ constexpr Df df_const(double d) { return Df{(float)d, (float)(d - (double)(float)d)}; }
 __device__ __forceinline__ Df df_mul(Df a, Df b) {
     const float p = a.hi * b.hi;
     float e = fmaf(a.hi, b.hi, -p);
@@ -168,6 +170,16 @@ struct Rodas3Coef {
     __device__ static constexpr double e(const DevArgs &, int i) { return i == 3 ? 1.0 : 0.0; }
     __device__ static constexpr double gamma0(const DevArgs &) { return 0.5; }
     __device__ static constexpr bool new_f(const DevArgs &, int) { return true; }
+    // a and c as double-float constants (the mixed lanes' stage loop indexes them at run time;
+    // selecting among constants keeps the FP64 pipe out of it)
+    __device__ static Df a_df(const DevArgs &, int i) {
+        constexpr Df two = df_const(2.0), one = df_const(1.0), zero = df_const(0.0);
+        return i == 1 || i == 3 ? two : i == 5 ? one : zero;
+    }
+    __device__ static Df c_df(const DevArgs &, int i) {
+        constexpr Df c0 = df_const(4.0), c1 = df_const(1.0), c2 = df_const(-1.0), c5 = df_const(-8.0 / 3.0);
+        return i == 0 ? c0 : i == 1 || i == 3 ? c1 : i == 2 || i == 4 ? c2 : c5;
+    }
 };
 
 // Any method of up to KIN_MAX_STAGES stages; the stage count is a runtime bound.
@@ -181,6 +193,8 @@ struct RuntimeCoef {
     __device__ static double e(const DevArgs &A, int i) { return A.me[i]; }
     __device__ static double gamma0(const DevArgs &A) { return A.gamma0; }
     __device__ static bool new_f(const DevArgs &A, int i) { return A.new_f[i] != 0; }
+    __device__ static Df a_df(const DevArgs &A, int i) { return df_from(A.ma[i]); }
+    __device__ static Df c_df(const DevArgs &A, int i) { return df_from(A.mc[i]); }
 };
 
 template <bool B, class X, class Y> struct Pick { typedef X type; };
@@ -961,6 +975,32 @@ __device__ __forceinline__ Df df_times_coef_u(Df a, double c) {
     if (c == -1.0 || c == 2.0 || c == -2.0 || c == 4.0 || c == -4.0 || c == 0.5 || c == -0.5) return df_scale(a, (float)c);
     return df_mul_u(a, df_from(c));
 }
+// df_times_coef_u with the coefficient already split (c = df_from of the FP64 value): the same
+// branches and results, decided by FP32 compares
+__device__ __forceinline__ Df df_times_coef_df_u(Df a, Df c) {
+    if (c.lo == 0.0f) {
+        if (c.hi == 1.0f) return a;
+        if (c.hi == -1.0f || c.hi == 2.0f || c.hi == -2.0f || c.hi == 4.0f || c.hi == -4.0f || c.hi == 0.5f || c.hi == -0.5f)
+            return df_scale(a, c.hi);
+    }
+    return df_mul_u(a, c);
+}
+
+// The mixed lanes' step-size factor (kin_solver.h:169-180's formula): for order 3 the cube
+// root comes from the FP32 chain of cbrt_clamped, then one division-free Newton step in FP64
+// for w = e^(-1/3) (w <- w (4 - e w^3) / 3, relative error ~2e-14 from FP32's ~1e-7), and
+// fac = 0.9 w -- a few FP64 operations instead of the six FP64 square roots and three FP64
+// divisions of the FP64 lanes. Orders 2 and 4 as step_factor.
+__device__ __forceinline__ double step_factor_mixed(double err, uint32_t order) {
+    if (order != 3) return step_factor(err, order);
+    const double e = vmin(vmax(err, 1e-4), 1e4);
+    const float g = cbrt_clamped((float)e);
+    double w = (double)(1.0f / g);
+    const double w3 = w * w * w;
+    w = w * (4.0 - e * w3) * (1.0 / 3.0);
+    const double fac = 0.9 * w;
+    return vmin(vmax(fac, 0.2), 6.0);
+}
 
 // kLuStride > 0: the FP32 LU lives in shared memory, interleaved across the CTA's lanes
 // (element e of lane t at [e * kLuStride + t]), which frees registers for the double-float vectors.
@@ -1165,8 +1205,10 @@ struct LaneIr {
         const double h_wanted = vmax(h, A.ctl.h_min);
         const bool last = h_wanted >= remaining;
         const double hs = last ? remaining : vmin(h_wanted, h_cap);
-        const double ghinv = 1.0 / (hs * M::gamma0(A)), hinv = 1.0 / hs;
-        const Df gd = df_from(ghinv);
+        const double hinv = 1.0 / hs;
+        // 1 / (gamma h): for gamma = 1/2 the same bits as 2 (1 / h), one FP64 division saved
+        const double ghinv = M::gamma0(A) == 0.5 ? 2.0 * hinv : 1.0 / (hs * M::gamma0(A));
+        const Df gd = df_from(ghinv), hd = df_from(hinv);
 
         // FP32 -J at the FP32 rounding of y, factorised
         if constexpr (kLuStride > 0) {
@@ -1196,14 +1238,14 @@ struct LaneIr {
 #pragma unroll
                 for (int j = 0; j < S - 1; ++j) {
                     if (j >= st) break;
-                    const double a = M::a(A, packed + j);
-                    if (a == 0.0) continue;
+                    const Df a = M::a_df(A, packed + j);
+                    if (a.hi == 0.0f) continue;
                     moved = true;
                     float kh[N], kl[N];
                     k_load(j, kh, kl);
                     for (int s = 0; s < N; ++s) {
                         if (s >= (int)nn) break;
-                        const Df v = df_acc(Df{Yhi[s], Ylo[s]}, df_times_coef_u(Df{kh[s], kl[s]}, a));
+                        const Df v = df_acc(Df{Yhi[s], Ylo[s]}, df_times_coef_df_u(Df{kh[s], kl[s]}, a));
                         Yhi[s] = v.hi;
                         Ylo[s] = v.lo;
                     }
@@ -1230,9 +1272,9 @@ struct LaneIr {
 #pragma unroll
             for (int j = 0; j < S - 1; ++j) {
                 if (j >= st) break;
-                const double c = M::c(A, packed + j);
-                if (c == 0.0) continue;
-                const Df ch = df_from(c * hinv);
+                const Df c = M::c_df(A, packed + j);
+                if (c.hi == 0.0f) continue;
+                const Df ch = df_mul(c, hd);   // c / h in double-float
                 float kh[N], kl[N];
                 k_load(j, kh, kl);
                 for (int s = 0; s < N; ++s) {
@@ -1314,7 +1356,7 @@ struct LaneIr {
         }
         double err = sqrt(df_to(err2) * (1.0 / (double)nn));
         if (!is_finite_lane(err)) err = 1e10;
-        double fac = step_factor(err, M::order(A));
+        double fac = step_factor_mixed(err, M::order(A));
         bool ok = err <= 1.0 || hs <= A.ctl.h_min;
         if (A.ctl.fixed_step) {
             ok = true;
