@@ -214,8 +214,8 @@ FP32_LANES_SM = 128          # FP32 lanes per SM
 # executes, so the bench scales it to its own launch -- and, for the mixed lanes, the FP32 flops
 # executed (FADD + FMUL + 2 FFMA thread instructions; FP32 work per algorithmic flop is high
 # because the state, right-hand sides and residuals are double-float).
-DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 506.8}
-MIXED_FP32_FLOPS_PER_CELL_STEP = 31683.0
+DRAM_BYTES_PER_CELL_STEP = {"f64": 4673.7, "mixed": 67.6}
+MIXED_FP32_FLOPS_PER_CELL_STEP = 31841.0
 PIPELINE_CHUNKS = (2, 4)   # lane-chunk counts tried for the pipelined end-to-end call (8 and 16 measured slower)
 
 
@@ -1029,7 +1029,7 @@ def run_large_mechanism(args):
     duration = args.duration
     pm = sg.Model.synthetic(seed=args.seed, species=200, reactions=1200, bimolecular=0.7, products=1,
                             lk_lo=-3.0, lk_hi=9.0)
-    ctl = sg.control(rtol=1e-4, atol=1e-12, h_min=1e-14, h_start=1e-9, max_steps=200000)
+    ctl = sg.control(**MECH200_CONTROL)
     z = sg.synthetic_cells(pm, cells, seed=args.seed + 1, log10_c=(-10.0, -3.0))
     mod = sg.Module(0, 2 * z.nbytes + (256 << 20))
     mod.coop_set_mech(pm, sg.method("rodas3"), ctl)
@@ -1118,6 +1118,9 @@ def run_large_mechanism(args):
 # shipped one; in the served mix their size and horizon are capped at these values so that the
 # whole stream finishes in minutes (the cap is recorded in the JSON line).
 SERVE_MECH200_MAX_CELLS, SERVE_MECH200_MAX_STEPS = 2048, 2
+# Step control of the 200-species synthetic mechanism (concentrations in its own units, 1e-10 .. 1e-3):
+# the shipped mechanism's atol (6.022e8 molecules/cm^3) would leave some of its cells to max_steps.
+MECH200_CONTROL = dict(rtol=1e-4, atol=1e-12, h_min=1e-14, h_start=1e-9, max_steps=200000)
 
 
 def serve_sample(seed: int, count: int, rate_hz: float = 200.0, mix: bool = True):
@@ -1149,8 +1152,8 @@ SERVE_STREAM_LIMIT_S = 900.0
 def _serve_stream(sg, reqs, inputs, prec, budget_bytes=0, big_model=None):
     """Submits every request at its arrival time and drives the engine until all are done."""
     with sg.Server(budget_bytes) as srv:
-        if big_model is not None:
-            srv.set_coop_mech(big_model)
+        if big_model is not None:   # its requests under the large-mechanism control (its own units)
+            srv.set_coop_mech(big_model, ctl=sg.control(**MECH200_CONTROL))
         srv.submit(inputs[0][0][:, :1024], inputs[0][1][:, :1024], 1, 256, 0.05, precision=prec,
                    mechanism=reqs[0]["mechanism"])   # warm-up: kernels loaded, pools primed
         srv.drain(timeout_s=300)
@@ -1171,7 +1174,7 @@ def _serve_stream(sg, reqs, inputs, prec, budget_bytes=0, big_model=None):
             if now >= next_report:   # progress on stderr; a stream that stops progressing ends the run
                 print(f"serve precision {prec} budget {budget_bytes}: {now:.0f} s, submitted {nxt}, running {running}, "
                       f"waiting {waiting}, finished {finished}", file=sys.stderr, flush=True)
-                next_report += 10.0
+                next_report = now + 10.0
                 if now > SERVE_STREAM_LIMIT_S:
                     raise RuntimeError(f"served stream not done after {now:.0f} s ({running} running, {waiting} waiting)")
             time.sleep(1e-4)

@@ -434,8 +434,9 @@ SGB_API int32_t gpu_serve_open(uint64_t hbm_budget_bytes, const KinControl *cont
 /* Table mechanism (mechanism = 1) and its method; only while the engine is empty. */
 SGB_API int32_t gpu_serve_set_mech(const KinMech *mech, const KinMethod *method);
 /* Large mechanism (mechanism = 2) from a finalized host model, up to 256 species; only while
- * the engine is empty. */
-SGB_API int32_t gpu_serve_set_coop_mech(const KinModelHandle *model, const KinMethod *method);
+ * the engine is empty. control: the step control of its requests (tolerances in the model's own
+ * concentration units); NULL = the engine's control of gpu_serve_open. */
+SGB_API int32_t gpu_serve_set_coop_mech(const KinModelHandle *model, const KinMethod *method, const KinControl *control);
 /* Queues a request; cudaErrorMemoryAllocation if it could never fit the budget. */
 SGB_API int32_t gpu_serve_submit(const GpuServeRequest *request, uint64_t *id);
 /* One scheduling round, non-blocking apart from uploads of newly admitted and

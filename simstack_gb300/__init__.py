@@ -197,7 +197,7 @@ def lib() -> C.CDLL:
             "gpu_serve_open": (i32, [u64, C.POINTER(KinControl)]),
             "gpu_serve_set_mech": (i32, [C.POINTER(KinMech), C.POINTER(KinMethod)]),
             "gpu_serve_submit": (i32, [C.POINTER(GpuServeRequest), C.POINTER(u64)]),
-            "gpu_serve_set_coop_mech": (i32, [vp, C.POINTER(KinMethod)]),
+            "gpu_serve_set_coop_mech": (i32, [vp, C.POINTER(KinMethod), C.POINTER(KinControl)]),
             "gpu_serve_progress": (i32, [C.POINTER(u32), C.POINTER(u32), C.POINTER(u32)]),
             "gpu_serve_cancel": (i32, [u64]),
             "gpu_serve_poll": (i32, [u64, C.POINTER(GpuServeStatus)]),
@@ -743,11 +743,13 @@ class Server:
         check(lib().gpu_serve_set_mech(C.byref(km), C.byref(meth)), "gpu_serve_set_mech")
         self._table_shape = (int(km.species_count), int(km.reaction_count))
 
-    def set_coop_mech(self, model: "Model", meth: KinMethod | None = None) -> None:
-        """Large mechanism for requests with mechanism = 2 (cooperative kernels)."""
+    def set_coop_mech(self, model: "Model", meth: KinMethod | None = None, ctl: KinControl | None = None) -> None:
+        """Large mechanism for requests with mechanism = 2 (cooperative kernels); ctl = its step
+        control in the model's own units (None: the engine's control)."""
         meth = meth if meth is not None else method("rodas3")
-        self._coop = (model, meth)
-        check(lib().gpu_serve_set_coop_mech(model.h, C.byref(meth)), "gpu_serve_set_coop_mech")
+        self._coop = (model, meth, ctl)
+        check(lib().gpu_serve_set_coop_mech(model.h, C.byref(meth), C.byref(ctl) if ctl is not None else None),
+              "gpu_serve_set_coop_mech")
         self._coop_shape = (model.n, model.R)
 
     def submit(self, y0: np.ndarray, k: np.ndarray, coupling_steps: int, channel_cells: int, velocity_m_s: float,

@@ -1235,7 +1235,7 @@ struct LaneIr {
                     Yhi[s] = yhi[s];
                     Ylo[s] = ylo[s];
                 }
-#pragma unroll
+#pragma unroll 1   // one copy of the body: the smaller step code is faster (1,048,576 cells x 10 s: 509.5 vs 520.7 ms)
                 for (int j = 0; j < S - 1; ++j) {
                     if (j >= st) break;
                     const Df a = M::a_df(A, packed + j);
@@ -1269,7 +1269,7 @@ struct LaneIr {
                 bhi[s] = fhi[s];
                 blo[s] = flo[s];
             }
-#pragma unroll
+#pragma unroll 1   // as above
             for (int j = 0; j < S - 1; ++j) {
                 if (j >= st) break;
                 const Df c = M::c_df(A, packed + j);

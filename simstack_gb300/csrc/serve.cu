@@ -183,6 +183,7 @@ struct Engine {
     void *d_coop_image = nullptr;   // mechanism 2
     CoopMech coop_head;
     KinMethod coop_method;
+    KinControl coop_control;        // mechanism 2's step control (its own concentration units)
     bool have_coop = false;
     KinControl control;
     int sms = 0;
@@ -277,7 +278,7 @@ cudaError_t admit(Request *r) {
     A.padded = P;
     A.lanes = q.cells;
     A.duration = q.dt;
-    A.ctl = E.control;
+    A.ctl = r->coop ? E.coop_control : E.control;
     const KinMethod M = r->generated ? method_coefficients(2) : r->coop ? E.coop_method : E.table_method;
     memcpy(A.ma, M.a, sizeof(A.ma));
     memcpy(A.mc, M.c, sizeof(A.mc));
@@ -433,7 +434,7 @@ SGB_API int32_t gpu_serve_set_mech(const KinMech *mech, const KinMethod *method)
 
 // Large mechanism (mechanism = 2, the cooperative kernels) from a finalized host model; only
 // while the engine is empty.
-SGB_API int32_t gpu_serve_set_coop_mech(const KinModelHandle *model, const KinMethod *method) {
+SGB_API int32_t gpu_serve_set_coop_mech(const KinModelHandle *model, const KinMethod *method, const KinControl *control) {
     if (!E.open || !model || !method || method->stages < 2 || method->stages > 4) return (int32_t)cudaErrorInvalidValue;
     if (!E.running.empty() || !E.waiting.empty()) return (int32_t)cudaErrorNotReady;
     const Model *m = model_of(model);
@@ -453,6 +454,7 @@ SGB_API int32_t gpu_serve_set_coop_mech(const KinModelHandle *model, const KinMe
     if (e != cudaSuccess) return (int32_t)e;
     E.coop_head = h;
     E.coop_method = *method;
+    E.coop_control = control ? *control : E.control;
     E.have_coop = true;
     return 0;
 }

@@ -184,7 +184,10 @@ def test_invalid_requests():
 def test_served_large_mechanism(oracle_lib, precision):
     """mechanism = 2: a 60-species / 300-reaction synthetic mechanism through the
     cooperative kernel inside the coupling graph; FP64 bit for bit against the
-    oracle's coupled computation, mixed within tolerance."""
+    oracle's coupled computation, mixed within tolerance. The engine keeps its
+    default control (the shipped mechanism's atol in molecules/cm^3); the large
+    mechanism's requests run under the control given with it (atol 1e-12 in its
+    own units), which the bit-for-bit comparison checks."""
     pm = sg.Model.synthetic(seed=7, species=60, reactions=300, bimolecular=0.7, products=1)
     om = oracle_lib.Mechanism()
     for s in range(60):
@@ -195,8 +198,8 @@ def test_served_large_mechanism(oracle_lib, precision):
     cells, cc, steps, v = 40, 16, 2, 0.05
     z = sg.synthetic_cells(pm, cells, seed=8)
     ctl = sg.control(rtol=1e-4, atol=1e-12, max_steps=200000)
-    with sg.Server(0, ctl) as srv:
-        srv.set_coop_mech(pm, sg.method("rodas3"))
+    with sg.Server(0) as srv:
+        srv.set_coop_mech(pm, sg.method("rodas3"), ctl)
         rid = srv.submit(z["y"][:, :cells], z["k"][:, :cells], steps, cc, v, precision=precision, mechanism=2)
         srv.drain(timeout_s=300)
         st = srv.poll(rid)
