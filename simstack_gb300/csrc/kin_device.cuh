@@ -919,7 +919,7 @@ struct LaneDf {
 // one refinement sweep per stage, whose residual r = b - ghinv x + J x is formed
 // in double-float with J x evaluated reaction by reaction at y (no stored
 // Jacobian). Only t, h and a few scalars per step are FP64. Its results track
-// the FP64 path to ~1e-8 (config-1 inputs, 1 s) where an FP32 solve alone
+// the FP64 path to ~1e-8 (4,096 cells of the shipped mechanism, 1 s) where an FP32 solve alone
 // leaves ~1e-3 on species near atol.
 
 __device__ __forceinline__ Df df_mul_f(Df a, float b) {   // double-float times float
